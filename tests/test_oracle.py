@@ -1,0 +1,119 @@
+"""The CPU oracle against the golden vectors produced by the reference's own CPU classes."""
+
+import numpy as np
+import pytest
+
+import oracle
+import golden_io
+
+CASES = golden_io.names()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_reference_goldens(name):
+    g = golden_io.load(name)
+    pts, qs, k, r2 = g["points"], g["queries"], g["k"], g["max_dist2"]
+    trees = {}
+    by_tag = {r["tag"]: r for r in g["runs"]}
+    for run in g["runs"]:
+        kind, skips, heap, fma = run["kind"], run["skips"], bool(run["heap"]), bool(run["fma"])
+        if fma:
+            # The contracted build of the reference fuses `acc += d*d` only where the host
+            # compiler chose to (it does at D <= 16; at D = 32 and 128 it vectorises the product
+            # instead).  Where that build came out identical to the plain one, it is plain
+            # arithmetic and is compared with the oracle's plain mode.
+            twin = by_tag[run["tag"][:-1] + "0"]
+            if np.array_equal(twin["dist"].view(np.uint32), run["dist"].view(np.uint32)) and \
+                    np.array_equal(twin["idx"], run["idx"]):
+                fma = False
+        if kind == "bf":
+            idx, dist = oracle.bf_knn(pts, qs, k, r2, heap=heap, fma=fma)
+            # Brute force inserts in index order, so even heap order is reproduced exactly.
+            assert np.array_equal(idx, run["idx"]), (name, run["tag"])
+            assert np.array_equal(dist.view(np.uint32), run["dist"].view(np.uint32)), (name, run["tag"])
+            continue
+        if run["fma"] and not np.array_equal(by_tag[run["tag"][:-1] + "0"]["idx"], run["idx"]) \
+                and name.startswith("ties"):
+            # Exact ties plus `>=` pruning make the returned tie members depend on the tree
+            # shape, and in the contracted build the shape depends on where the compiler fused
+            # the variance sums.  Check what ties cannot change: each row's sorted distances.
+            _, want = oracle.split_keys(oracle.row_keys(*oracle.bf_knn(pts, qs, k, r2, fma=True)))
+            _, got = oracle.split_keys(oracle.row_keys(run["idx"], run["dist"]))
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (name, run["tag"])
+            continue
+        key = (kind, skips, fma)
+        if key not in trees:
+            trees[key] = (oracle.kd_tree(pts, skips) if kind == "kd"
+                          else oracle.ball_tree(pts, skips, fma=fma))
+        # strict=False restates the reference's `>=` pruning, so ties resolve the same way.
+        idx, dist = trees[key].knn(qs, k, r2, heap=heap, fma=fma, strict=False)
+        assert np.array_equal(oracle.row_keys(idx, dist), oracle.row_keys(run["idx"], run["dist"])), \
+            (name, run["tag"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_strict_trees_equal_brute_force(name):
+    """With pruning on `bound > k-th` the trees return brute force's key-ordered top-k."""
+    g = golden_io.load(name)
+    pts, qs, k, r2 = g["points"], g["queries"], g["k"], g["max_dist2"]
+    want = oracle.row_keys(*oracle.bf_knn(pts, qs, k, r2))
+    for kind in ("kd", "ball"):
+        for skips in (0, 1, 3):
+            t = oracle.kd_tree(pts, skips) if kind == "kd" else oracle.ball_tree(pts, skips)
+            got = oracle.row_keys(*t.knn(qs, k, r2, strict=True))
+            assert np.array_equal(got, want), (name, kind, skips)
+
+
+def test_fma_and_plain_modes_differ_by_few_ulp():
+    g = golden_io.load("ball_d16_k32_sub")
+    a = g["runs"][-2]  # bf fma0
+    b = g["runs"][-1]  # bf fma1
+    assert a["tag"].endswith("fma0") and b["tag"].endswith("fma1")
+    _, da = oracle.split_keys(oracle.row_keys(a["idx"], a["dist"]))
+    _, db = oracle.split_keys(oracle.row_keys(b["idx"], b["dist"]))
+    assert oracle.ulp_distance(da, db).max() <= 4
+
+
+def test_tree_shape_matches_reference_rules():
+    # levels = log2Ceil(n) - skips, leaves of 2^skips slots (src/KnnTrees.cuh:84-93,
+    # src/KdTree.cuh:56-61); the ball tree forces skips >= 1 (src/BallTree.cuh:124).
+    assert oracle.tree_shape(4194304, 0) == (22, 1, (1 << 22) - 1)
+    assert oracle.tree_shape(1048576, 1, ball=True) == (19, 2, (1 << 19) - 1)
+    assert oracle.tree_shape(1048576, 0, ball=True) == (19, 2, (1 << 19) - 1)
+    assert oracle.tree_shape(100000, 3) == (14, 8, (1 << 14) - 1)
+    assert oracle.tree_shape(1, 5) == (1, 1, 1)
+    assert oracle.tree_shape(3, 4) == (1, 2, 1)
+
+
+def _round_f32(x):
+    """Round an exact rational to the nearest float32 (ties to even)."""
+    from fractions import Fraction
+    f = np.float32(float(x))  # within one float32 ulp of x
+    best = None
+    for c in (np.nextafter(f, np.float32(-np.inf)), f, np.nextafter(f, np.float32(np.inf))):
+        err = abs(Fraction(float(c)) - x)
+        even = (int(np.array(c, np.float32).view(np.uint32)) & 1) == 0
+        if best is None or err < best[0] or (err == best[0] and even):
+            best = (err, c)
+    return np.float32(best[1])
+
+
+def _fma_dist2_exact(a, b):
+    """acc = fma(t, t, acc) in dimension order, each step rounded once from the exact value."""
+    from fractions import Fraction
+    acc = np.float32(0.0)
+    for x, y in zip(a, b):
+        t = np.float32(x) - np.float32(y)  # float32 subtraction, one rounding
+        acc = _round_f32(Fraction(float(t)) * Fraction(float(t)) + Fraction(float(acc)))
+    return acc
+
+
+@pytest.mark.parametrize("dims", [1, 3, 16, 32, 128])
+def test_oracle_fma_mode_is_a_single_rounding_per_step(dims):
+    rng = np.random.default_rng(dims)
+    for _ in range(40):
+        a = rng.standard_normal(dims).astype(np.float32)
+        b = rng.standard_normal(dims).astype(np.float32)
+        want = _fma_dist2_exact(a, b)
+        got = np.float32(oracle.dist2(a, b, fma=True))
+        assert got.view(np.uint32) == want.view(np.uint32)
