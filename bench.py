@@ -1,0 +1,395 @@
+"""Benchmark of the exact-kNN engine on GB300: exact kNN queries/sec.
+
+Default workload (the configuration the headline metric is quoted on): KdTreeGpu<3>,
+depthSkips 0, N = 4,194,304 points from a 64-component Gaussian mixture (sigma 0.01),
+Q = 1,048,576 queries from the same mixture, K = 16, max radius +inf; seeded synthetic data.
+
+One step = one exact query pass over the Q queries on the prebuilt tree (construction is timed
+once and reported separately).  Timed steps: CUDA events on the query stream, L2 flushed (a
+256 MB write) before every step, synchronize + barrier on both sides, max over ranks.
+
+Reported:
+  value      queries/sec of the chosen form (engine-selected plan), inputs resident in HBM;
+  e2e        the same through the C ABI with pinned HOST buffers (knn_query_host: copies of the
+             queries in and the results out inside the timed region);
+  plain      queries/sec of the plain form (the caller's template arguments, no autotune);
+  roofline   bytes the dominant search kernel must move per launch (visit counts from the
+             device counters x node/leaf/query/result sizes) / its CUDA-event time, against the
+             measured HBM bandwidth;
+  cpu_baseline  the reference algorithm on the host cores (oracle port of src/KdTree.cuh), all
+             threads, over the full query set.
+
+`--impl reference` times the reference's CPU implementation of the same workload instead.
+Multi-GPU (`--gpus N` under torchrun): independent replicas, one per GPU (the path has no
+exchange step); value = all ranks' queries / the slowest rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from cudaexactknn_gb300 import workloads as W  # noqa: E402
+
+L2_FLUSH_BYTES = 256 << 20
+METRIC = "exact kNN queries/sec on 1 GB300: chosen vs plain GPU form, 100% exact match"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (debug only)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str, workload: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", f"ncu_{kernel}_{workload}.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch:"):
+            return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                mhz.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not mhz:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(mhz)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, value: float) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload(args):
+    return W.CONFIGS[args.workload](args.scale)
+
+
+def tree_kind_label(w):
+    return {"bf": f"BruteForceGpu<{w.dims}>", "kd": f"KdTreeGpu<{w.dims}>", "ball": f"BallTreeGpu<{w.dims}>"}[w.structure]
+
+
+def algorithmic_bytes(w, counters, count):
+    """Bytes per launch by the per-query figure: nodes x node size + leaf slots x slot size +
+    query + result row.  k-d node = 4 B split; ball visit = two child balls; slot = 4(D+1) B."""
+    d = w.dims
+    slot = 4 * (d + 1)
+    if w.structure == "kd":
+        node_b = 4
+    elif w.structure == "ball":
+        node_b = 2 * 4 * (d + 1)
+    else:
+        node_b = 0
+    per_result = 8 * w.k
+    if w.structure == "bf":
+        return count * (4 * d + per_result) + w.points.shape[0] * 4 * d, 0
+    total = counters.nodes_visited * node_b + counters.points_scanned * slot + count * (4 * d + per_result)
+    floor = count * (4 * d + per_result) + w.points.shape[0] * slot
+    return total, floor
+
+
+def cpu_baseline(w, threads, sample=None):
+    import oracle
+    qs = w.queries if sample is None else w.queries[:sample]
+    t0 = time.perf_counter()
+    if w.structure == "kd":
+        tree = oracle.kd_tree(w.points, w.depth_skips)
+    elif w.structure == "ball":
+        tree = oracle.ball_tree(w.points, w.depth_skips)
+    else:
+        tree = None
+    build_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    if tree is None:
+        oracle.bf_knn(w.points, qs, w.k, w.max_dist2, heap=w.heap, fma=True, threads=threads)
+    else:
+        tree.knn(qs, w.k, w.max_dist2, heap=w.heap, fma=True, strict=False, threads=threads)
+    dt = time.perf_counter() - t0
+    return len(qs) / dt, build_s, len(qs)
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    w = workload(args)
+    threads = os.cpu_count() or 1
+    import oracle
+    kind = "port"
+    sample = {"c1": None, "c2": 262144, "c3": 4096, "c4": 64}[args.workload]
+    label = {"kd": "KdTree", "ball": "BallTree", "bf": "BruteForce"}[w.structure]
+    if w.structure == "kd":
+        tree = oracle.kd_tree(w.points, w.depth_skips)
+    elif w.structure == "ball":
+        tree = oracle.ball_tree(w.points, w.depth_skips)
+    else:
+        tree = None
+    qs = w.queries if sample is None else w.queries[:sample]
+
+    def step():
+        if tree is None:
+            oracle.bf_knn(w.points, qs, w.k, w.max_dist2, heap=w.heap, fma=True, threads=threads)
+        else:
+            tree.knn(qs, w.k, w.max_dist2, heap=w.heap, fma=True, strict=False, threads=threads)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    qps = len(qs) * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w.name, "structure": f"{label}<{w.dims}> (CPU)", "k": w.k,
+                   "depth_skips": w.depth_skips, "queries_per_step": len(qs)},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": kind,
+                         "sample": f"{len(qs)} of {len(w.queries)} queries per step, "
+                                   f"oracle port of src/{label}.cuh, {threads} host threads"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    from cudaexactknn_gb300 import _lib, knn
+    import oracle
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = workload(args)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+
+    pts = torch.from_numpy(w.points).to(dev)
+    qs = torch.from_numpy(w.queries).to(dev)
+    count, k = len(w.queries), w.k
+    index = knn.build_index(w.structure, pts, w.depth_skips)
+    build_ms = index.info().build_ms
+    out_i = torch.empty((count, k), dtype=torch.int32, device=dev)
+    out_d = torch.empty((count, k), dtype=torch.float32, device=dev)
+    query = knn.Query(qs, count, w.max_dist2, out_i, out_d)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    plain_kw = dict(block_size=32 if w.structure != "ball" else 16, heap=w.heap)
+    chosen_kw = dict(block_size=128, heap=False)
+
+    def timed(kw, steps, warmup):
+        for _ in range(warmup):
+            index.batch_knn(query, k, sync=False, **kw)
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        kern_ms = []
+        launches0 = lib.knn_launch_count()
+        for s in range(steps):
+            flush.zero_()
+            ev[s][0].record(stream)
+            index.batch_knn(query, k, sync=False, flags=_lib.QF_TIMING, **kw)
+            ev[s][1].record(stream)
+            tot = ctypes_float()
+            ker = ctypes_float()
+            _lib.check(lib.knn_last_query_timing(index.handle, ctypes.byref(tot), ctypes.byref(ker)))
+            kern_ms.append(ker.value)
+        torch.cuda.synchronize(dev)
+        launches = lib.knn_launch_count() - launches0
+        barrier(world)
+        total_ms = sum(a.elapsed_time(b) for a, b in ev)
+        return total_ms, float(np.mean(kern_ms)), launches
+
+    import ctypes
+    ctypes_float = ctypes.c_float
+
+    # Exactness of both forms on a sample, checked against the CPU oracle (outside timing).
+    sample = np.random.default_rng(0).choice(count, size=min(count, 2048), replace=False)
+    want = oracle.row_keys(*oracle.bf_knn(w.points, w.queries[sample], k, w.max_dist2, fma=True,
+                                          threads=os.cpu_count() or 1))
+    exact = {}
+    for name, kw in (("plain", plain_kw), ("chosen", chosen_kw)):
+        index.batch_knn(query, k, **kw)
+        got = oracle.row_keys(out_i[sample].cpu().numpy(), out_d[sample].cpu().numpy())
+        exact[name] = float((got == want).all(axis=1).mean())
+
+    counters = index.stats(query, k, **plain_kw)
+    alg_bytes, floor_bytes = algorithmic_bytes(w, counters, count)
+
+    with ClockSampler(local) as clocks:
+        chosen_ms, chosen_kern_ms, launches = timed(chosen_kw, args.steps, args.warmup)
+    plain_ms, plain_kern_ms, _ = timed(plain_kw, args.steps, max(1, args.warmup // 2))
+    chosen_ms = max_over_ranks(world, chosen_ms)
+    plain_ms = max_over_ranks(world, plain_ms)
+    value = world * count * args.steps / (chosen_ms / 1e3)
+    plain_qps = world * count * args.steps / (plain_ms / 1e3)
+
+    # End to end through the C ABI with pinned host buffers.
+    h_q = torch.from_numpy(w.queries).pin_memory()
+    h_i = torch.empty((count, k), dtype=torch.int32).pin_memory()
+    h_d = torch.empty((count, k), dtype=torch.float32).pin_memory()
+    for _ in range(args.warmup):
+        index.knn_host(h_q, k, w.max_dist2, h_i, h_d, **chosen_kw)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        index.knn_host(h_q, k, w.max_dist2, h_i, h_d, **chosen_kw)
+        e2e_s += time.perf_counter() - t0
+    e2e_s = max_over_ranks(world, e2e_s)
+    e2e_qps = world * count * args.steps / e2e_s
+    e2e_exact = float((oracle.row_keys(h_i.numpy()[sample], h_d.numpy()[sample]) == want).all(axis=1).mean())
+
+    peak, peak_kind = peaks()
+    kernel_name = {"kd": "kd_knn_kernel", "ball": "ball_knn_kernel", "bf": "bf_knn_kernel"}[w.structure]
+    achieved = alg_bytes / (chosen_kern_ms / 1e3) / 1e9
+    traffic = profile_traffic(kernel_name, args.workload)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": chosen_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, shapes of the config)",
+        "config": {"workload": w.name, "structure": tree_kind_label(w), "n": int(w.points.shape[0]),
+                   "queries": count, "k": k, "depth_skips": w.depth_skips, "max_distance2": "inf",
+                   "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
+        "exact_match": {"chosen": exact["chosen"], "plain": exact["plain"], "e2e": e2e_exact,
+                        "sample_queries": int(len(sample))},
+        "plain": {"value": plain_qps, "ms_per_step": plain_ms / args.steps, "plan": plain_kw,
+                  "kernel_ms": plain_kern_ms},
+        "chosen": {"plan": chosen_kw, "kernel_ms": chosen_kern_ms, "speedup_vs_plain": value / plain_qps},
+        "build_ms": build_ms,
+        "e2e": {"value": e2e_qps, "unit": "queries/s",
+                "h2d_bytes_per_step": int(w.queries.nbytes),
+                "d2h_bytes_per_step": int(count * k * 8)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "kernel": kernel_name, "algorithmic_bytes_per_launch": int(alg_bytes),
+                     "compulsory_bytes_per_launch": int(floor_bytes),
+                     "visits": {"nodes": int(counters.nodes_visited), "leaves": int(counters.leaves_visited),
+                                "points": int(counters.points_scanned)}},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample_q = {"c1": None, "c2": None, "c3": 16384, "c4": 256}[args.workload]
+        qps, build_s, nq = cpu_baseline(w, threads, sample_q)
+        line["cpu_baseline"] = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                                "sample": f"{nq} of {count} queries, oracle port of the reference's CPU "
+                                          f"{w.structure} algorithm, {threads} threads (tree build {build_s:.1f} s, untimed)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    index.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,133 @@
+"""ctypes binding of the engine's C ABI (include/cudaexactknn.h).
+
+The shared library is built in-tree by ``cudaexactknn_gb300.build`` (or ``__graft_entry__.build``).
+There is no fallback: if the library is missing, ``load()`` raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "libcudaexactknn.so")
+HEADER = os.path.join(ROOT, "include", "cudaexactknn.h")
+
+# Status codes (enum knn_status).
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_UNSUPPORTED = 2
+ERR_CUDA = 3
+ERR_OUT_OF_MEMORY = 4
+ERR_DEVICE_LIMIT = 5
+ERR_NOT_TRAINED = 6
+
+BRUTE_FORCE, KD_TREE, BALL_TREE = 0, 1, 2
+
+QF_SYNC = 1
+QF_AUTOTUNE = 2
+QF_LEARNED_RADIUS = 4
+QF_BF16_FILTER = 8
+QF_KEEP_ORDER = 16
+QF_TIMING = 32
+
+
+class QueryOpts(ctypes.Structure):
+    _fields_ = [("block_size", ctypes.c_uint32), ("heap_tracking", ctypes.c_uint32),
+                ("shmem_tracking", ctypes.c_uint32), ("shmem_stack", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32), ("leaf_scan", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 2)]
+
+
+class QueryCounters(ctypes.Structure):
+    _fields_ = [("nodes_visited", ctypes.c_uint64), ("leaves_visited", ctypes.c_uint64),
+                ("points_scanned", ctypes.c_uint64), ("fallback_queries", ctypes.c_uint64),
+                ("reserved", ctypes.c_uint64 * 4)]
+
+
+class IndexInfo(ctypes.Structure):
+    _fields_ = [("structure", ctypes.c_uint32), ("n", ctypes.c_uint32), ("dims", ctypes.c_uint32),
+                ("aux_dims", ctypes.c_uint32), ("depth_skips", ctypes.c_uint32),
+                ("node_depth", ctypes.c_uint32), ("leaf_slots", ctypes.c_uint32),
+                ("node_count", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64),
+                ("build_ms", ctypes.c_float), ("radius_model", ctypes.c_uint32)]
+
+
+class KnnError(RuntimeError):
+    """A non-zero knn_status; ``.status`` holds the code (the reference throws CudaException)."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{message} [status {status}]")
+        self.status = status
+
+
+_vp = ctypes.c_void_p
+_u32 = ctypes.c_uint32
+_f = ctypes.c_float
+_pp = ctypes.POINTER(ctypes.c_void_p)
+
+_SIGNATURES = {
+    "knn_bf_create": [_vp, _u32, _u32, _vp, _pp],
+    "knn_kd_create": [_vp, _u32, _u32, _u32, _u32, _u32, _vp, _pp],
+    "knn_ball_create": [_vp, _u32, _u32, _u32, _u32, _vp, _pp],
+    "knn_destroy": [_vp],
+    "knn_index_get_info": [_vp, ctypes.POINTER(IndexInfo)],
+    "knn_query": [_vp, _vp, _u32, _f, _u32, _vp, _vp, ctypes.POINTER(QueryOpts), _vp],
+    "knn_query_radii": [_vp, _vp, _u32, _vp, _u32, _vp, _vp, ctypes.POINTER(QueryOpts), _vp],
+    "knn_query_host": [_vp, _vp, _u32, _f, _u32, _vp, _vp, ctypes.POINTER(QueryOpts), _vp],
+    "knn_query_stats": [_vp, _vp, _u32, _f, _u32, _vp, _vp, ctypes.POINTER(QueryOpts), _vp,
+                        ctypes.POINTER(QueryCounters)],
+    "knn_last_query_timing": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
+    "knn_launch_count": [],
+    "knn_status_string": [ctypes.c_int],
+    "knn_last_error": [],
+    "knn_version": [],
+}
+
+_lib = None
+
+
+def header_symbols() -> list[str]:
+    """Names of the functions include/cudaexactknn.h declares."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"KNN_API\s+(?:const\s+char\s*\*|int|uint64_t)\s+(knn_\w+)\s*\(", text)))
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, args in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        if name in ("knn_status_string", "knn_last_error"):
+            fn.restype = ctypes.c_char_p
+        elif name == "knn_launch_count":
+            fn.restype = ctypes.c_uint64
+        else:
+            fn.restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != OK:
+        lib = load()
+        raise KnnError(status, lib.knn_last_error().decode(errors="replace") or
+                       lib.knn_status_string(status).decode())
+
+
+def opts(block_size=0, heap=False, shmem_tracking=False, shmem_stack=False, flags=0, leaf_scan=0) -> QueryOpts:
+    o = QueryOpts()
+    o.block_size = block_size
+    o.heap_tracking = int(bool(heap))
+    o.shmem_tracking = int(bool(shmem_tracking))
+    o.shmem_stack = int(bool(shmem_stack))
+    o.flags = flags
+    o.leaf_scan = leaf_scan
+    return o

@@ -1,0 +1,237 @@
+// Ball tree query kernels, one translation unit per padded dimension count (KNN_DP).
+//
+// Replaces BallTreeKernels::knnDevice and its four storage variants (src/BallTreeGpu.cuh:36-200).
+// Same depth-first search: at each internal node measure the query's distance to both child
+// balls, descend into the closer one, push the farther one when it can still hold a neighbour,
+// stop the descent when even the closer ball is out of range (src/BallTreeGpu.cuh:82-92).
+// The reference's border distance sqrt(d2) - r (with -use_fast_math's approximate sqrt) can
+// round above a point's own float distance and prune a true neighbour; here knn::ball_bound
+// uses directed rounding and relative margins so it never exceeds the float dist2 of any point
+// in the ball, and a ball is pruned only when its bound > the k-th distance.
+
+#include <algorithm>
+
+#include "tree_query.cuh"
+
+#ifndef KNN_DP
+#error "compile with -DKNN_DP=<padded dims>"
+#endif
+
+namespace knn {
+
+struct BallParams {
+    const float* ball;     // node i: centre (DP floats), radius at [DP]
+    uint32_t ball_stride;
+    const float* leaf;
+    uint32_t leaf_stride;
+    uint32_t node_count;
+    uint32_t leaf_slots;
+    float margin;
+    const float* queries;
+    uint32_t dims;
+    uint32_t nq;
+    const uint32_t* order;
+    float max_d2;
+    const float* radii;
+    uint32_t k;
+    int32_t* out_idx;
+    float* out_dist;
+    DevCounters* counters;
+};
+
+// Float dist2 from q to a ball's centre; the radius comes back through *r.
+template <int DP>
+__device__ __forceinline__ float centre_dist(const float (&q)[DP], const float* __restrict__ b, float* r) {
+    if constexpr (DP < 4) {
+        const float4 v = *reinterpret_cast<const float4*>(b);
+        const float w[4] = {v.x, v.y, v.z, v.w};
+        *r = w[DP];
+        float acc = 0.0f;
+#pragma unroll
+        for (int d = 0; d < DP; ++d) {
+            const float t = __fsub_rn(q[d], w[d]);
+            acc = __fmaf_rn(t, t, acc);
+        }
+        return acc;
+    } else {
+        *r = b[DP];
+        return dist2_vec4<DP>(q, reinterpret_cast<const float4*>(b));
+    }
+}
+
+template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
+__global__ void __launch_bounds__(256) ball_knn_kernel(const BallParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.nq) return;  // no block-wide barriers below
+    uint64_t* sh_nn = reinterpret_cast<uint64_t*>(smem);
+    uint32_t* sh_st = reinterpret_cast<uint32_t*>(smem + tracker_smem_bytes(SHNN, KMAX, blockDim.x));
+
+    const uint32_t qi = p.order ? p.order[t] : t;
+    float q[DP];
+    load_query<DP>(p.queries, p.dims, qi, q);
+    const float r2 = p.radii ? p.radii[qi] : p.max_d2;
+
+    Tracker<KMAX, HEAP, SHNN> tr;
+    tr.init(p.k, r2, sh_nn + threadIdx.x, blockDim.x);
+    Stack<SHST> st;
+    st.init(sh_st, blockDim.x);
+    st.push(0, 0.0f);
+    LocalCounters lc;
+    bool overflow = false;
+
+    while (st.top) {
+        uint32_t node;
+        float bound;
+        st.pop(&node, &bound);
+        if (bound > tr.radius()) continue;
+        bool pruned = false;
+        while (node < p.node_count) {
+            const uint32_t l = 2 * node + 1;
+            float rl, rr;
+            const float sl = centre_dist<DP>(q, p.ball + static_cast<size_t>(l) * p.ball_stride, &rl);
+            const float sr = centre_dist<DP>(q, p.ball + static_cast<size_t>(l + 1) * p.ball_stride, &rr);
+            const float bl = ball_bound(sl, rl, p.margin);
+            const float br = ball_bound(sr, rr, p.margin);
+            ++lc.nodes;
+            // Visit order only (not a bound): the nearer border first.
+            const bool left_first = sqrtf(sl) - rl < sqrtf(sr) - rr;
+            const uint32_t close_child = left_first ? l : l + 1;
+            const float close_b = left_first ? bl : br;
+            const float far_b = left_first ? br : bl;
+            if (close_b > tr.radius()) {
+                // The farther ball's bound is at least as large in the common case, but the
+                // order above is approximate, so it is checked on its own.
+                if (far_b <= tr.radius()) {
+                    node = left_first ? l + 1 : l;
+                    continue;
+                }
+                pruned = true;
+                break;
+            }
+            if (far_b <= tr.radius()) overflow |= !st.push(left_first ? l + 1 : l, far_b);
+            node = close_child;
+        }
+        if (pruned) continue;
+        const float* slot = p.leaf + static_cast<size_t>(node - p.node_count) * p.leaf_slots * p.leaf_stride;
+        ++lc.leaves;
+        for (uint32_t s = 0; s < p.leaf_slots; ++s, slot += p.leaf_stride) {
+            int32_t id;
+            const float d2 = slot_dist<DP>(q, slot, &id);
+            if (id < 0) break;
+            ++lc.points;
+            tr.offer(make_key(d2, id));
+        }
+    }
+    tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
+    if (p.counters) {
+        lc.flush(p.counters);
+        if (overflow) atomicExch(&p.counters->error, 1);
+    }
+}
+
+// Sort key of a query: the node reached after `levels` steps towards the nearer child centre.
+template <int DP>
+__global__ void ball_leaf_key_kernel(const float* __restrict__ ball, uint32_t ball_stride, uint32_t levels,
+                                     const float* __restrict__ queries, uint32_t dims, uint32_t nq,
+                                     uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nq) return;
+    float q[DP];
+    load_query<DP>(queries, dims, t, q);
+    uint32_t node = 0;
+    for (uint32_t d = 0; d < levels; ++d) {
+        const uint32_t l = 2 * node + 1;
+        float rl, rr;
+        const float sl = centre_dist<DP>(q, ball + static_cast<size_t>(l) * ball_stride, &rl);
+        const float sr = centre_dist<DP>(q, ball + static_cast<size_t>(l + 1) * ball_stride, &rr);
+        node = sl <= sr ? l : l + 1;
+    }
+    keys[t] = node - ((1u << levels) - 1u);
+    vals[t] = t;
+}
+
+template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
+static int launch_ball(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order,
+                       cudaStream_t s) {
+    const uint32_t block = plan.block ? plan.block : 128;
+    const size_t smem = tracker_smem_bytes(SHNN, KMAX, block) + stack_smem_bytes(SHST, block);
+    auto kern = ball_knn_kernel<DP, KMAX, HEAP, SHNN, SHST>;
+    if (smem > 48 * 1024)
+        KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    BallParams p{};
+    p.ball = ix->ball.as<float>();
+    p.ball_stride = ix->ball_stride;
+    p.leaf = ix->leaf.as<float>();
+    p.leaf_stride = ix->leaf_stride;
+    p.node_count = ix->node_count;
+    p.leaf_slots = ix->leaf_slots;
+    p.margin = rel_margin(ix->dims);
+    p.queries = a.queries;
+    p.dims = ix->dims;
+    p.nq = a.count;
+    p.order = order;
+    p.max_d2 = a.max_d2;
+    p.radii = a.radii;
+    p.k = a.k;
+    p.out_idx = a.out_idx;
+    p.out_dist = a.out_dist;
+    p.counters = a.counters;
+    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));
+    kern<<<ceil_div(a.count, block), block, smem, s>>>(p);
+    KNN_LAUNCHED();
+    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
+    return KNN_OK;
+}
+
+template <int DP, int KMAX>
+static int launch_ball_variant(knn_index* ix, const QueryArgs& a, const QueryPlan& p, const uint32_t* order,
+                               cudaStream_t s) {
+#define KNN_BALL_CASE(H, N, S)                                          \
+    if (p.heap == H && p.sh_nn == N && p.sh_stack == S)                 \
+        return launch_ball<DP, KMAX, H, N, S>(ix, a, p, order, s);
+    KNN_BALL_CASE(false, false, false)
+    KNN_BALL_CASE(false, false, true)
+    KNN_BALL_CASE(false, true, false)
+    KNN_BALL_CASE(false, true, true)
+    KNN_BALL_CASE(true, false, false)
+    KNN_BALL_CASE(true, false, true)
+    KNN_BALL_CASE(true, true, false)
+    KNN_BALL_CASE(true, true, true)
+#undef KNN_BALL_CASE
+    return fail(KNN_ERR_INVALID_ARGUMENT, "bad query plan");
+}
+
+template <uint32_t DP>
+int ball_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s) {
+    const uint32_t* order = nullptr;
+    const uint32_t levels = std::min<uint32_t>(ix->node_depth, 24);
+    if (p.reorder && a.count >= 4096 && levels > 0) {
+        const size_t nq = a.count;
+        const size_t need = carve_bytes({nq * 4, nq * 4, nq * 4, nq * 4, radix_sort_temp_bytes(a.count)});
+        KNN_TRY(ix->workspace.reserve(need));
+        Carver c(ix->workspace.ptr);
+        uint32_t* keys = c.take<uint32_t>(nq);
+        uint32_t* vals = c.take<uint32_t>(nq);
+        uint32_t* keys_alt = c.take<uint32_t>(nq);
+        uint32_t* vals_alt = c.take<uint32_t>(nq);
+        void* temp = c.take<uint8_t>(radix_sort_temp_bytes(a.count));
+        ball_leaf_key_kernel<DP><<<ceil_div(a.count, 256), 256, 0, s>>>(ix->ball.as<float>(), ix->ball_stride, levels,
+                                                                        a.queries, ix->dims, a.count, keys, vals);
+        KNN_LAUNCHED();
+        bool in_alt = false;
+        KNN_TRY(radix_sort_pairs(keys, vals, keys_alt, vals_alt, a.count, static_cast<int>(levels), temp, s, &in_alt));
+        order = in_alt ? vals_alt : vals;
+    }
+    switch (k_class(a.k)) {
+        case 8: return launch_ball_variant<DP, 8>(ix, a, p, order, s);
+        case 16: return launch_ball_variant<DP, 16>(ix, a, p, order, s);
+        case 32: return launch_ball_variant<DP, 32>(ix, a, p, order, s);
+        case 64: return launch_ball_variant<DP, 64>(ix, a, p, order, s);
+        default: return launch_ball_variant<DP, 128>(ix, a, p, order, s);
+    }
+}
+
+template int ball_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
+
+}  // namespace knn

@@ -1,0 +1,328 @@
+// C ABI of the engine (include/cudaexactknn.h): argument checks, tree shape rules, dispatch to
+// the structure implementations, and per-thread error messages.  Nothing here throws across
+// the ABI; every failure is a knn_status code plus knn_last_error().
+
+#include <cstdio>
+#include <cstring>
+#include <atomic>
+#include <new>
+
+#include "knn_internal.h"
+
+namespace {
+
+thread_local char g_last_error[512] = "";
+
+}  // namespace
+
+namespace knn {
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+
+void note_launches(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    const char* base = std::strrchr(file, '/');
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s (%s:%d)", cudaGetErrorString(e), what,
+                  base ? base + 1 : file, line);
+    return e == cudaErrorMemoryAllocation ? KNN_ERR_OUT_OF_MEMORY : KNN_ERR_CUDA;
+}
+
+}  // namespace knn
+
+using knn::fail;
+
+namespace {
+
+cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+int check_points(const float* d_points, uint32_t n, uint32_t dims) {
+    if (dims == 0) return fail(KNN_ERR_INVALID_ARGUMENT, "dims must be >= 1");
+    if (dims > knn::kMaxDims) return fail(KNN_ERR_UNSUPPORTED, "dims %u > %u", dims, knn::kMaxDims);
+    if (n > 0x7FFFFFFFu) return fail(KNN_ERR_UNSUPPORTED, "n %u >= 2^31", n);
+    if (n > 0 && !d_points) return fail(KNN_ERR_INVALID_ARGUMENT, "points is null");
+    return KNN_OK;
+}
+
+// Tree shape from n and depthSkips (src/KdTreeGpu.cuh:375-380, src/BallTreeGpu.cuh:614-619).
+void tree_shape(knn_index* ix, uint32_t skips, bool ball) {
+    const uint32_t l2 = knn::log2_ceil(ix->n);
+    uint32_t s = ball ? (skips < 1 ? 1 : skips) : skips;
+    if (s > l2 - 1) s = l2 - 1;
+    ix->skips = s;
+    ix->node_depth = l2 - s;
+    ix->leaf_slots = 1u << s;
+    ix->node_count = (1u << ix->node_depth) - 1;
+}
+
+template <class BuildFn>
+int create_common(knn_index* ix, cudaStream_t s, BuildFn&& build) {
+    cudaGetDevice(&ix->device);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    int rc = ix->n ? build() : KNN_OK;
+    if (rc == KNN_OK) {
+        cudaEventRecord(e1, s);
+        const cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) rc = knn::cuda_fail(e, "construction", __FILE__, __LINE__);
+        else cudaEventElapsedTime(&ix->build_ms, e0, e1);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == KNN_OK) rc = ix->counters.alloc(sizeof(knn::DevCounters));
+    return rc;
+}
+
+int finish_create(knn_index* ix, int rc, knn_index** out) {
+    if (rc != KNN_OK) {
+        delete ix;
+        *out = nullptr;
+        return rc;
+    }
+    *out = ix;
+    return KNN_OK;
+}
+
+int make_plan(const knn_index* ix, const knn_query_opts* o, knn::QueryPlan* p) {
+    *p = knn::QueryPlan{};
+    if (!o) return KNN_OK;
+    if (o->block_size) {
+        if (o->block_size > 256)
+            return fail(KNN_ERR_INVALID_ARGUMENT, "block_size %u: at most 256", o->block_size);
+        p->block = o->block_size;
+    }
+    p->heap = o->heap_tracking != 0;
+    p->sh_nn = o->shmem_tracking != 0;
+    p->sh_stack = o->shmem_stack != 0;
+    p->reorder = (o->flags & KNN_QF_KEEP_ORDER) == 0;
+    p->timing = (o->flags & KNN_QF_TIMING) != 0;
+    p->leaf_scan = o->leaf_scan;
+    (void)ix;
+    return KNN_OK;
+}
+
+int run_query(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts, cudaStream_t s) {
+    if (!ix) return fail(KNN_ERR_INVALID_ARGUMENT, "index is null");
+    if (a.k == 0) return fail(KNN_ERR_INVALID_ARGUMENT, "k must be >= 1");
+    if (a.k > knn::kMaxK) return fail(KNN_ERR_UNSUPPORTED, "k %u > %u", a.k, knn::kMaxK);
+    if (!a.radii && !(a.max_d2 >= 0.0f)) return fail(KNN_ERR_INVALID_ARGUMENT, "max_distance2 must be >= 0 (got %g)", a.max_d2);
+    if (a.count > 0x7FFFFFFFu) return fail(KNN_ERR_UNSUPPORTED, "count %u >= 2^31", a.count);
+    if (a.count == 0) return KNN_OK;
+    if (!a.queries || !a.out_idx || !a.out_dist) return fail(KNN_ERR_INVALID_ARGUMENT, "null query or result pointer");
+    const uint32_t flags = opts ? opts->flags : 0;
+    if (flags & KNN_QF_LEARNED_RADIUS) {
+        if (!ix->has_model) return fail(KNN_ERR_NOT_TRAINED, "no radius model attached to this index");
+    }
+    knn::QueryPlan plan;
+    KNN_TRY(make_plan(ix, opts, &plan));
+    if (plan.timing) {
+        KNN_TRY(ix->timing.ensure());
+        ix->timing.valid = false;
+        KNN_TRY_CUDA(cudaEventRecord(ix->timing.total0, s));
+        KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));  // empty kernel span if none runs
+        KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
+    }
+    int rc;
+    if (ix->n == 0) {
+        rc = knn::fill_empty_rows(a, s);
+    } else {
+        switch (ix->structure) {
+            case KNN_BRUTE_FORCE: rc = knn::bf_query(ix, a, plan, s); break;
+            case KNN_KD_TREE: rc = knn::kd_query(ix, a, plan, s); break;
+            case KNN_BALL_TREE: rc = knn::ball_query(ix, a, plan, s); break;
+            default: rc = fail(KNN_ERR_INVALID_ARGUMENT, "unknown structure"); break;
+        }
+    }
+    if (rc != KNN_OK) return rc;
+    if (plan.timing) {
+        KNN_TRY_CUDA(cudaEventRecord(ix->timing.total1, s));
+        ix->timing.valid = true;
+    }
+    if (flags & KNN_QF_SYNC) KNN_TRY_CUDA(cudaStreamSynchronize(s));
+    return KNN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int knn_bf_create(const float* d_points, uint32_t n, uint32_t dims, void* stream, knn_index** out) {
+    if (!out) return fail(KNN_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    KNN_TRY(check_points(d_points, n, dims));
+    auto* ix = new (std::nothrow) knn_index();
+    if (!ix) return fail(KNN_ERR_OUT_OF_MEMORY, "host allocation failed");
+    ix->structure = KNN_BRUTE_FORCE;
+    ix->n = n;
+    ix->dims = dims;
+    ix->dp = knn::padded_dims(dims);
+    ix->aux_dims = dims;
+    cudaStream_t s = as_stream(stream);
+    const int rc = create_common(ix, s, [&] { return knn::bf_build(ix, d_points, s); });
+    return finish_create(ix, rc, out);
+}
+
+int knn_kd_create(const float* d_points, uint32_t n, uint32_t dims, uint32_t aux_dims, uint32_t depth_skips,
+                  uint32_t build_block, void* stream, knn_index** out) {
+    if (!out) return fail(KNN_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    KNN_TRY(check_points(d_points, n, dims));
+    if (aux_dims == 0 || aux_dims > dims)
+        return fail(KNN_ERR_INVALID_ARGUMENT, "aux_dims %u must be in [1, dims=%u]", aux_dims, dims);
+    auto* ix = new (std::nothrow) knn_index();
+    if (!ix) return fail(KNN_ERR_OUT_OF_MEMORY, "host allocation failed");
+    ix->structure = KNN_KD_TREE;
+    ix->n = n;
+    ix->dims = dims;
+    ix->dp = knn::padded_dims(dims);
+    ix->aux_dims = aux_dims;
+    if (n) tree_shape(ix, depth_skips, false);
+    cudaStream_t s = as_stream(stream);
+    const int rc = create_common(ix, s, [&] { return knn::kd_build(ix, d_points, build_block, s); });
+    return finish_create(ix, rc, out);
+}
+
+int knn_ball_create(const float* d_points, uint32_t n, uint32_t dims, uint32_t depth_skips, uint32_t build_block,
+                    void* stream, knn_index** out) {
+    if (!out) return fail(KNN_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    KNN_TRY(check_points(d_points, n, dims));
+    auto* ix = new (std::nothrow) knn_index();
+    if (!ix) return fail(KNN_ERR_OUT_OF_MEMORY, "host allocation failed");
+    ix->structure = KNN_BALL_TREE;
+    ix->n = n;
+    ix->dims = dims;
+    ix->dp = knn::padded_dims(dims);
+    ix->aux_dims = dims;
+    if (n) tree_shape(ix, depth_skips, true);
+    cudaStream_t s = as_stream(stream);
+    const int rc = create_common(ix, s, [&] { return knn::ball_build(ix, d_points, build_block, s); });
+    return finish_create(ix, rc, out);
+}
+
+int knn_destroy(knn_index* index) {
+    if (!index) return KNN_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    const int dev = index->device;
+    if (prev != dev) cudaSetDevice(dev);
+    delete index;
+    if (prev != dev) cudaSetDevice(prev);
+    return KNN_OK;
+}
+
+int knn_index_get_info(const knn_index* ix, knn_index_info* out) {
+    if (!ix || !out) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    out->structure = static_cast<uint32_t>(ix->structure);
+    out->n = ix->n;
+    out->dims = ix->dims;
+    out->aux_dims = ix->aux_dims;
+    out->depth_skips = ix->skips;
+    out->node_depth = ix->node_depth;
+    out->leaf_slots = ix->leaf_slots;
+    out->node_count = ix->node_count;
+    out->device_bytes = ix->device_bytes;
+    out->build_ms = ix->build_ms;
+    out->radius_model = ix->has_model ? 1u : 0u;
+    return KNN_OK;
+}
+
+int knn_query(knn_index* index, const float* d_queries, uint32_t count, float max_distance2, uint32_t k,
+              int32_t* d_indexes, float* d_distances, const knn_query_opts* opts, void* stream) {
+    knn::QueryArgs a{d_queries, count, max_distance2, nullptr, k, d_indexes, d_distances, nullptr};
+    return run_query(index, a, opts, as_stream(stream));
+}
+
+int knn_query_radii(knn_index* index, const float* d_queries, uint32_t count, const float* d_max_distance2,
+                    uint32_t k, int32_t* d_indexes, float* d_distances, const knn_query_opts* opts, void* stream) {
+    if (!d_max_distance2) return fail(KNN_ERR_INVALID_ARGUMENT, "radii is null");
+    knn::QueryArgs a{d_queries, count, 0.0f, d_max_distance2, k, d_indexes, d_distances, nullptr};
+    return run_query(index, a, opts, as_stream(stream));
+}
+
+int knn_query_host(knn_index* index, const float* h_queries, uint32_t count, float max_distance2, uint32_t k,
+                   int32_t* h_indexes, float* h_distances, const knn_query_opts* opts, void* stream) {
+    if (!index) return fail(KNN_ERR_INVALID_ARGUMENT, "index is null");
+    if (count == 0) return KNN_OK;
+    if (!h_queries || !h_indexes || !h_distances) return fail(KNN_ERR_INVALID_ARGUMENT, "null host pointer");
+    if (k == 0 || k > knn::kMaxK) return fail(k == 0 ? KNN_ERR_INVALID_ARGUMENT : KNN_ERR_UNSUPPORTED, "k %u", k);
+    cudaStream_t s = as_stream(stream);
+    const size_t qb = static_cast<size_t>(count) * index->dims * sizeof(float);
+    const size_t rb = static_cast<size_t>(count) * k * sizeof(int32_t);
+    KNN_TRY(index->staging.reserve(knn::carve_bytes({qb, rb, rb})));
+    knn::Carver c(index->staging.ptr);
+    float* dq = c.take<float>(static_cast<size_t>(count) * index->dims);
+    int32_t* di = c.take<int32_t>(static_cast<size_t>(count) * k);
+    float* dd = c.take<float>(static_cast<size_t>(count) * k);
+    KNN_TRY_CUDA(cudaMemcpyAsync(dq, h_queries, qb, cudaMemcpyHostToDevice, s));
+    knn::QueryArgs a{dq, count, max_distance2, nullptr, k, di, dd, nullptr};
+    KNN_TRY(run_query(index, a, opts, s));
+    KNN_TRY_CUDA(cudaMemcpyAsync(h_indexes, di, rb, cudaMemcpyDeviceToHost, s));
+    KNN_TRY_CUDA(cudaMemcpyAsync(h_distances, dd, rb, cudaMemcpyDeviceToHost, s));
+    KNN_TRY_CUDA(cudaStreamSynchronize(s));
+    return KNN_OK;
+}
+
+int knn_query_stats(knn_index* index, const float* d_queries, uint32_t count, float max_distance2, uint32_t k,
+                    int32_t* d_indexes, float* d_distances, const knn_query_opts* opts, void* stream,
+                    knn_query_counters* out) {
+    if (!index || !out) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
+    cudaStream_t s = as_stream(stream);
+    auto* dc = index->counters.as<knn::DevCounters>();
+    KNN_TRY_CUDA(cudaMemsetAsync(dc, 0, sizeof(knn::DevCounters), s));
+    knn::QueryArgs a{d_queries, count, max_distance2, nullptr, k, d_indexes, d_distances, dc};
+    KNN_TRY(run_query(index, a, opts, s));
+    knn::DevCounters hc{};
+    KNN_TRY_CUDA(cudaMemcpyAsync(&hc, dc, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    KNN_TRY_CUDA(cudaStreamSynchronize(s));
+    std::memset(out, 0, sizeof(*out));
+    out->nodes_visited = hc.nodes;
+    out->leaves_visited = hc.leaves;
+    out->points_scanned = hc.points;
+    out->fallback_queries = hc.fallback;
+    if (hc.error) return fail(KNN_ERR_DEVICE_LIMIT, "a query kernel's stack bound check fired");
+    return KNN_OK;
+}
+
+int knn_last_query_timing(knn_index* index, float* total_ms, float* kernel_ms) {
+    if (!index || !total_ms || !kernel_ms) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
+    if (!index->timing.valid) return fail(KNN_ERR_INVALID_ARGUMENT, "no timed query on this index");
+    KNN_TRY_CUDA(cudaEventSynchronize(index->timing.total1));
+    KNN_TRY_CUDA(cudaEventElapsedTime(total_ms, index->timing.total0, index->timing.total1));
+    KNN_TRY_CUDA(cudaEventElapsedTime(kernel_ms, index->timing.kern0, index->timing.kern1));
+    return KNN_OK;
+}
+
+uint64_t knn_launch_count(void) { return knn::g_launches.load(); }
+
+const char* knn_status_string(int status) {
+    switch (status) {
+        case KNN_OK: return "ok";
+        case KNN_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case KNN_ERR_UNSUPPORTED: return "unsupported size";
+        case KNN_ERR_CUDA: return "CUDA error";
+        case KNN_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case KNN_ERR_DEVICE_LIMIT: return "device bounds check fired";
+        case KNN_ERR_NOT_TRAINED: return "no radius model";
+        default: return "unknown status";
+    }
+}
+
+const char* knn_last_error(void) { return g_last_error; }
+
+int knn_version(void) { return 10000; }
+
+}  // extern "C"

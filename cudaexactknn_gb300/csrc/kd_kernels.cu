@@ -1,0 +1,199 @@
+// k-d tree query kernels, one translation unit per padded dimension count (KNN_DP).
+//
+// Replaces KdTreeKernels::knnDevice and its four storage variants (src/KdTreeGpu.cuh:37-184).
+// Same depth-first search: descend to the closer child, push the farther child with the squared
+// distance to its splitting plane, scan leaves, pop.  Differences:
+//   * queries are reordered so that neighbouring threads descend to neighbouring leaves (sorted
+//     by the leaf each query reaches), which keeps a warp's node and leaf loads together;
+//   * the plane bound fl((q[dim]-split)^2) never exceeds the float distance of any point
+//     beyond the plane (float subtraction and rounding are monotone and every term of the
+//     fused sum is non-negative), and nodes are pruned only when bound > k-th distance, so no
+//     point whose key could enter the top-k is skipped, ties included;
+//   * k-th key cached in a register; tracker/stack storage chosen by the plan.
+
+#include <algorithm>
+
+#include "tree_query.cuh"
+
+#ifndef KNN_DP
+#error "compile with -DKNN_DP=<padded dims>"
+#endif
+
+namespace knn {
+
+struct KdParams {
+    const float* split;
+    const float* leaf;
+    uint32_t leaf_stride;
+    uint32_t node_count;
+    uint32_t leaf_slots;
+    uint32_t aux;
+    const float* queries;
+    uint32_t dims;
+    uint32_t nq;
+    const uint32_t* order;  // thread -> query, or null
+    float max_d2;
+    const float* radii;
+    uint32_t k;
+    int32_t* out_idx;
+    float* out_dist;
+    DevCounters* counters;
+};
+
+template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
+__global__ void __launch_bounds__(256) kd_knn_kernel(const KdParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.nq) return;  // no block-wide barriers below
+    uint64_t* sh_nn = reinterpret_cast<uint64_t*>(smem);
+    uint32_t* sh_st = reinterpret_cast<uint32_t*>(smem + tracker_smem_bytes(SHNN, KMAX, blockDim.x));
+
+    const uint32_t qi = p.order ? p.order[t] : t;
+    float q[DP];
+    load_query<DP>(p.queries, p.dims, qi, q);
+    const float r2 = p.radii ? p.radii[qi] : p.max_d2;
+
+    Tracker<KMAX, HEAP, SHNN> tr;
+    tr.init(p.k, r2, sh_nn + threadIdx.x, blockDim.x);
+    Stack<SHST> st;
+    st.init(sh_st, blockDim.x);
+    st.push(0, 0.0f);
+    LocalCounters lc;
+    bool overflow = false;
+
+    while (st.top) {
+        uint32_t node;
+        float bound;
+        st.pop(&node, &bound);
+        if (bound > tr.radius()) continue;
+        uint32_t depth = heap_depth(node);
+        while (node < p.node_count) {
+            const uint32_t dim = depth % p.aux;
+            const float diff = __fsub_rn(pick<DP>(q, dim), __ldg(p.split + node));
+            const uint32_t l = 2 * node + 1;
+            const uint32_t close_child = diff < 0.0f ? l : l + 1;
+            const uint32_t far_child = diff < 0.0f ? l + 1 : l;
+            const float b = __fmul_rn(diff, diff);
+            if (b <= tr.radius()) overflow |= !st.push(far_child, b);
+            node = close_child;
+            ++depth;
+            ++lc.nodes;
+        }
+        const float* slot = p.leaf + static_cast<size_t>(node - p.node_count) * p.leaf_slots * p.leaf_stride;
+        ++lc.leaves;
+        for (uint32_t s = 0; s < p.leaf_slots; ++s, slot += p.leaf_stride) {
+            int32_t id;
+            const float d2 = slot_dist<DP>(q, slot, &id);
+            if (id < 0) break;
+            ++lc.points;
+            tr.offer(make_key(d2, id));
+        }
+    }
+    tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
+    if (p.counters) {
+        lc.flush(p.counters);
+        if (overflow) atomicExch(&p.counters->error, 1);
+    }
+}
+
+// Sort key of a query: the node it reaches after `levels` closer-child steps (path bits).
+template <int DP>
+__global__ void kd_leaf_key_kernel(const float* __restrict__ split, uint32_t aux, uint32_t levels,
+                                   const float* __restrict__ queries, uint32_t dims, uint32_t nq,
+                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nq) return;
+    float q[DP];
+    load_query<DP>(queries, dims, t, q);
+    uint32_t node = 0;
+    for (uint32_t d = 0; d < levels; ++d) {
+        const float diff = pick<DP>(q, d % aux) - __ldg(split + node);
+        node = 2 * node + (diff < 0.0f ? 1u : 2u);
+    }
+    keys[t] = node - ((1u << levels) - 1u);
+    vals[t] = t;
+}
+
+template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
+static int launch_kd(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order,
+                     cudaStream_t s) {
+    const uint32_t block = plan.block ? plan.block : 128;
+    const size_t smem = tracker_smem_bytes(SHNN, KMAX, block) + stack_smem_bytes(SHST, block);
+    auto kern = kd_knn_kernel<DP, KMAX, HEAP, SHNN, SHST>;
+    if (smem > 48 * 1024)
+        KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    KdParams p{};
+    p.split = ix->split.as<float>();
+    p.leaf = ix->leaf.as<float>();
+    p.leaf_stride = ix->leaf_stride;
+    p.node_count = ix->node_count;
+    p.leaf_slots = ix->leaf_slots;
+    p.aux = ix->aux_dims;
+    p.queries = a.queries;
+    p.dims = ix->dims;
+    p.nq = a.count;
+    p.order = order;
+    p.max_d2 = a.max_d2;
+    p.radii = a.radii;
+    p.k = a.k;
+    p.out_idx = a.out_idx;
+    p.out_dist = a.out_dist;
+    p.counters = a.counters;
+    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));
+    kern<<<ceil_div(a.count, block), block, smem, s>>>(p);
+    KNN_LAUNCHED();
+    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
+    return KNN_OK;
+}
+
+template <int DP, int KMAX>
+static int launch_kd_variant(knn_index* ix, const QueryArgs& a, const QueryPlan& p, const uint32_t* order,
+                             cudaStream_t s) {
+#define KNN_KD_CASE(H, N, S)                                            \
+    if (p.heap == H && p.sh_nn == N && p.sh_stack == S)                 \
+        return launch_kd<DP, KMAX, H, N, S>(ix, a, p, order, s);
+    KNN_KD_CASE(false, false, false)
+    KNN_KD_CASE(false, false, true)
+    KNN_KD_CASE(false, true, false)
+    KNN_KD_CASE(false, true, true)
+    KNN_KD_CASE(true, false, false)
+    KNN_KD_CASE(true, false, true)
+    KNN_KD_CASE(true, true, false)
+    KNN_KD_CASE(true, true, true)
+#undef KNN_KD_CASE
+    return fail(KNN_ERR_INVALID_ARGUMENT, "bad query plan");
+}
+
+template <uint32_t DP>
+int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s) {
+    const uint32_t* order = nullptr;
+    const uint32_t levels = std::min<uint32_t>(ix->node_depth, 24);
+    if (p.reorder && a.count >= 4096 && levels > 0) {
+        const size_t nq = a.count;
+        const size_t need = carve_bytes({nq * 4, nq * 4, nq * 4, nq * 4, radix_sort_temp_bytes(a.count)});
+        KNN_TRY(ix->workspace.reserve(need));
+        Carver c(ix->workspace.ptr);
+        uint32_t* keys = c.take<uint32_t>(nq);
+        uint32_t* vals = c.take<uint32_t>(nq);
+        uint32_t* keys_alt = c.take<uint32_t>(nq);
+        uint32_t* vals_alt = c.take<uint32_t>(nq);
+        void* temp = c.take<uint8_t>(radix_sort_temp_bytes(a.count));
+        kd_leaf_key_kernel<DP><<<ceil_div(a.count, 256), 256, 0, s>>>(ix->split.as<float>(), ix->aux_dims, levels,
+                                                                      a.queries, ix->dims, a.count, keys, vals);
+        KNN_LAUNCHED();
+        bool in_alt = false;
+        KNN_TRY(radix_sort_pairs(keys, vals, keys_alt, vals_alt, a.count, static_cast<int>(levels), temp, s, &in_alt));
+        order = in_alt ? vals_alt : vals;
+    }
+    switch (k_class(a.k)) {
+        case 8: return launch_kd_variant<DP, 8>(ix, a, p, order, s);
+        case 16: return launch_kd_variant<DP, 16>(ix, a, p, order, s);
+        case 32: return launch_kd_variant<DP, 32>(ix, a, p, order, s);
+        case 64: return launch_kd_variant<DP, 64>(ix, a, p, order, s);
+        default: return launch_kd_variant<DP, 128>(ix, a, p, order, s);
+    }
+}
+
+template int kd_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
+
+}  // namespace knn

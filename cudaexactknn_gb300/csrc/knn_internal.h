@@ -1,0 +1,236 @@
+// Internal declarations of the engine: the index object behind the C ABI, its device memory
+// layout, the scratch workspace, error plumbing and the per-structure entry points.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <initializer_list>
+#include <vector>
+
+#include "../../include/cudaexactknn.h"
+#include "knn_common.cuh"
+
+namespace knn {
+
+// ---- errors -----------------------------------------------------------------------------------
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define KNN_TRY_CUDA(expr)                                                          \
+    do {                                                                            \
+        cudaError_t knn_e_ = (expr);                                                \
+        if (knn_e_ != cudaSuccess) return ::knn::cuda_fail(knn_e_, #expr, __FILE__, __LINE__); \
+    } while (0)
+
+// Counts a kernel launch (or `n` of them) and checks the launch error.
+void note_launches(uint32_t n);
+#define KNN_LAUNCHED_N(n)                  \
+    do {                                   \
+        ::knn::note_launches(n);           \
+        KNN_TRY_CUDA(cudaGetLastError());  \
+    } while (0)
+#define KNN_LAUNCHED() KNN_LAUNCHED_N(1)
+
+#define KNN_TRY(expr)                   \
+    do {                                \
+        int knn_rc_ = (expr);           \
+        if (knn_rc_ != KNN_OK) return knn_rc_; \
+    } while (0)
+
+// ---- dimension padding ------------------------------------------------------------------------
+// Kernels are compiled for padded dimension counts; padded coordinates are zero in both points
+// and queries, so they add exactly 0 to every squared distance.
+constexpr uint32_t kMaxDims = 128;
+constexpr uint32_t kMaxK = 128;
+
+inline uint32_t padded_dims(uint32_t d) {
+    if (d <= 4) return d;
+    if (d <= 8) return 8;
+    if (d <= 16) return 16;
+    if (d <= 32) return 32;
+    if (d <= 64) return 64;
+    return 128;
+}
+
+inline uint32_t round_up4(uint32_t v) { return (v + 3u) & ~3u; }
+
+// Top-k capacity classes (run-time k <= KMAX).
+inline uint32_t k_class(uint32_t k) {
+    if (k <= 8) return 8;
+    if (k <= 16) return 16;
+    if (k <= 32) return 32;
+    if (k <= 64) return 64;
+    return 128;
+}
+
+// ---- device memory ------------------------------------------------------------------------------
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    int alloc(size_t n) {
+        release();
+        if (n == 0) return KNN_OK;
+        cudaError_t e = cudaMalloc(&ptr, n);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            ptr = nullptr;
+            return e == cudaErrorMemoryAllocation
+                       ? fail(KNN_ERR_OUT_OF_MEMORY, "cudaMalloc of %zu bytes failed", n)
+                       : cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
+        }
+        bytes = n;
+        return KNN_OK;
+    }
+    // Grow-only: keeps the current allocation when it is large enough.
+    int reserve(size_t n) { return n <= bytes ? KNN_OK : alloc(n); }
+    template <class T>
+    T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Bump allocator over one device buffer (256-byte aligned carve-outs).
+struct Carver {
+    char* base;
+    size_t off = 0;
+    explicit Carver(void* b) : base(static_cast<char*>(b)) {}
+    template <class T>
+    T* take(size_t count) {
+        off = (off + 255) & ~static_cast<size_t>(255);
+        T* p = reinterpret_cast<T*>(base + off);
+        off += count * sizeof(T);
+        return p;
+    }
+};
+inline size_t carve_bytes(std::initializer_list<size_t> sizes) {
+    size_t off = 0;
+    for (size_t s : sizes) off = ((off + 255) & ~static_cast<size_t>(255)) + s;
+    return off + 256;
+}
+
+// ---- device-side counters (instrumented query runs) -------------------------------------------
+struct DevCounters {
+    unsigned long long nodes;
+    unsigned long long leaves;
+    unsigned long long points;
+    unsigned long long fallback;
+    int error;      // a kernel's bounds check fired
+    int pad[7];
+};
+
+// ---- the index ----------------------------------------------------------------------------------
+struct QueryPlan {
+    uint32_t block = 0;      // threads per block
+    bool heap = false;
+    bool sh_nn = false;
+    bool sh_stack = false;
+    bool reorder = true;
+    bool timing = false;     // record events around the main search kernel
+    uint32_t leaf_scan = 0;  // 0 = tree leaves
+};
+
+// Events bracketing a query and its main search kernel (KNN_QF_TIMING).
+struct QueryTiming {
+    cudaEvent_t total0 = nullptr, total1 = nullptr, kern0 = nullptr, kern1 = nullptr;
+    bool valid = false;
+    ~QueryTiming() {
+        for (cudaEvent_t e : {total0, total1, kern0, kern1})
+            if (e) cudaEventDestroy(e);
+    }
+    int ensure() {
+        if (total0) return KNN_OK;
+        for (cudaEvent_t* e : {&total0, &total1, &kern0, &kern1}) KNN_TRY_CUDA(cudaEventCreate(e));
+        return KNN_OK;
+    }
+};
+
+}  // namespace knn
+
+struct knn_index {
+    int structure = KNN_BRUTE_FORCE;
+    int device = 0;
+    uint32_t n = 0, dims = 0, dp = 0, aux_dims = 0;
+    uint32_t skips = 0, node_depth = 0, leaf_slots = 0, node_count = 0;
+
+    // Brute force: points, padded to `point_stride` floats (a multiple of 4), zero padding.
+    knn::DevBuf points;
+    uint32_t point_stride = 0;
+
+    // k-d tree: split value per internal node (implicit heap, children 2i+1, 2i+2).
+    knn::DevBuf split;
+
+    // Trees: leaf slots, 2^node_depth leaves x leaf_slots slots; a slot is `leaf_stride` floats:
+    // coordinates (dp, zero padded) then the point index as int32 bits (-1 = empty slot).
+    knn::DevBuf leaf;
+    uint32_t leaf_stride = 0;
+    uint32_t leaf_id_at = 0;
+
+    // Ball tree: one ball per node of every level (root .. leaves), node i at
+    // ball + i * ball_stride: centre (dp floats), then radius.
+    knn::DevBuf ball;
+    uint32_t ball_stride = 0;
+
+    size_t device_bytes = 0;
+    float build_ms = 0.0f;
+
+    // Scratch for queries, grown on demand, reused across calls.
+    knn::DevBuf workspace;
+    knn::DevBuf staging;   // device copies of host queries/results (knn_query_host)
+    knn::DevBuf counters;  // DevCounters
+    knn::QueryTiming timing;
+
+    // Learned radius model (weights on the device), see radius_model.cu.
+    knn::DevBuf model;
+    bool has_model = false;
+    float model_scale = 1.0f;
+};
+
+namespace knn {
+
+// Stable LSD radix sort of (u32 key, u32 value) pairs over the low `key_bits` bits, 8 bits per
+// pass.  Ping-pongs between (keys, vals) and (keys_alt, vals_alt); returns which pair holds
+// the result via *in_alt.  `temp` must hold radix_sort_temp_bytes(n).
+size_t radix_sort_temp_bytes(uint32_t n);
+int radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt,
+                     uint32_t n, int key_bits, void* temp, cudaStream_t s, bool* in_alt);
+
+// Exclusive prefix sum of per-block counts: counts[rows][cols] row-major -> out, each row
+// scanned independently (one thread block per row).
+int scan_rows_exclusive(const uint32_t* counts, uint32_t* out, uint32_t rows, uint32_t cols,
+                        cudaStream_t s);
+
+// Structure entry points (bf.cu, kd.cu, ball.cu).
+int bf_build(knn_index* ix, const float* d_points, cudaStream_t s);
+int kd_build(knn_index* ix, const float* d_points, uint32_t build_block, cudaStream_t s);
+int ball_build(knn_index* ix, const float* d_points, uint32_t build_block, cudaStream_t s);
+
+struct QueryArgs {
+    const float* queries;     // [count][dims] device
+    uint32_t count;
+    float max_d2;
+    const float* radii;       // per-query max_distance2, or null
+    uint32_t k;
+    int32_t* out_idx;
+    float* out_dist;
+    DevCounters* counters;    // null unless instrumented
+};
+
+int bf_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
+int kd_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
+int ball_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
+
+// Rows of unfilled results (index -1, distance = radius) for an empty point set.
+int fill_empty_rows(const QueryArgs& a, cudaStream_t s);
+
+int sm_count();
+
+}  // namespace knn

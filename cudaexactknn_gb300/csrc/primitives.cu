@@ -1,0 +1,205 @@
+// Device primitives used by construction and query preparation: a stable LSD radix sort of
+// (u32 key, u32 value) pairs, per-row exclusive scans of block counts, and empty-result rows.
+//
+// The reference sorts with cub::DeviceRadixSort and scans with cub::DeviceScan
+// (src/KdTreeGpu.cuh:313-320, src/BallTreeGpu.cuh:500-505); the engine uses these instead.
+
+#include "knn_internal.h"
+
+namespace knn {
+
+namespace {
+
+constexpr uint32_t kSortThreads = 256;
+constexpr uint32_t kSortWarps = kSortThreads / 32;
+constexpr uint32_t kSortItemsPerWarp = 512;
+constexpr uint32_t kSortTile = kSortWarps * kSortItemsPerWarp;  // 4096 keys per block
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Per-block digit histogram, written digit-major: counts[digit * nblocks + block].
+__global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint32_t* __restrict__ keys,
+                                                                  uint32_t n, uint32_t shift,
+                                                                  uint32_t* __restrict__ counts,
+                                                                  uint32_t nblocks) {
+    __shared__ uint32_t h[kSortWarps][256];
+    const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    for (uint32_t i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&h[0][0])[i] = 0;
+    __syncthreads();
+    const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kSortTile + warp * kSortItemsPerWarp;
+    for (uint32_t it = 0; it < kSortItemsPerWarp; it += 32) {
+        const uint64_t idx = base + it + lane;
+        const bool valid = idx < n;
+        const uint32_t digit = valid ? (keys[idx] >> shift) & 255u : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+        if (valid && lane == static_cast<uint32_t>(__ffs(peers) - 1)) h[warp][digit] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    uint32_t total = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kSortWarps; ++w) total += h[w][threadIdx.x];
+    counts[static_cast<size_t>(threadIdx.x) * nblocks + blockIdx.x] = total;
+}
+
+// Stable scatter: each warp owns a contiguous sub-tile and walks it in order, so equal digits
+// keep their input order.
+__global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
+    const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n, uint32_t shift,
+    const uint32_t* __restrict__ offsets, uint32_t nblocks, uint32_t* __restrict__ keys_out,
+    uint32_t* __restrict__ vals_out) {
+    __shared__ uint32_t h[kSortWarps][256];
+    const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    for (uint32_t i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&h[0][0])[i] = 0;
+    __syncthreads();
+    const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kSortTile + warp * kSortItemsPerWarp;
+    for (uint32_t it = 0; it < kSortItemsPerWarp; it += 32) {
+        const uint64_t idx = base + it + lane;
+        const bool valid = idx < n;
+        const uint32_t digit = valid ? (keys[idx] >> shift) & 255u : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+        if (valid && lane == static_cast<uint32_t>(__ffs(peers) - 1)) h[warp][digit] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const uint32_t d = threadIdx.x;  // one digit per thread (256 threads)
+        uint32_t run = offsets[static_cast<size_t>(d) * nblocks + blockIdx.x];
+#pragma unroll
+        for (uint32_t w = 0; w < kSortWarps; ++w) {
+            const uint32_t c = h[w][d];
+            h[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    const uint32_t lt = lanemask_lt();
+    for (uint32_t it = 0; it < kSortItemsPerWarp; it += 32) {
+        const uint64_t idx = base + it + lane;
+        const bool valid = idx < n;
+        const uint32_t key = valid ? keys[idx] : 0u;
+        const uint32_t digit = valid ? (key >> shift) & 255u : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+        uint32_t pos = 0;
+        if (valid) pos = h[warp][digit] + __popc(peers & lt);
+        __syncwarp();
+        if (valid && lane == static_cast<uint32_t>(__ffs(peers) - 1)) h[warp][digit] += __popc(peers);
+        __syncwarp();
+        if (valid) {
+            keys_out[pos] = key;
+            vals_out[pos] = vals[idx];
+        }
+    }
+}
+
+// Exclusive scan of each row of a [rows][cols] u32 matrix; one block of 1024 threads per row,
+// each thread owning a contiguous chunk.
+__global__ void __launch_bounds__(1024) scan_rows_kernel(const uint32_t* __restrict__ in,
+                                                         uint32_t* __restrict__ out, uint32_t cols) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t* row_in = in + static_cast<size_t>(blockIdx.x) * cols;
+    uint32_t* row_out = out + static_cast<size_t>(blockIdx.x) * cols;
+    const uint32_t chunk = (cols + blockDim.x - 1) / blockDim.x;
+    const uint32_t lo = min(cols, threadIdx.x * chunk), hi = min(cols, lo + chunk);
+    uint32_t sum = 0;
+    for (uint32_t i = lo; i < hi; ++i) sum += row_in[i];
+    // Block-wide exclusive scan of the per-thread sums.
+    const uint32_t lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += v;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < blockDim.x / 32 ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= static_cast<uint32_t>(o)) w += v;
+        }
+        warp_sums[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    uint32_t run = incl - sum + (warp > 0 ? warp_sums[warp - 1] : 0);
+    for (uint32_t i = lo; i < hi; ++i) {
+        const uint32_t v = row_in[i];
+        row_out[i] = run;
+        run += v;
+    }
+}
+
+__global__ void fill_rows_kernel(uint32_t count, uint32_t k, float max_d2, const float* __restrict__ radii,
+                                 int32_t* __restrict__ idx, float* __restrict__ dist) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= static_cast<uint64_t>(count) * k) return;
+    idx[i] = -1;
+    dist[i] = radii ? radii[i / k] : max_d2;
+}
+
+}  // namespace
+
+size_t radix_sort_temp_bytes(uint32_t n) {
+    const size_t nblocks = (static_cast<size_t>(n) + kSortTile - 1) / kSortTile;
+    return 2 * 256 * nblocks * sizeof(uint32_t) + 512;
+}
+
+int radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt,
+                     uint32_t n, int key_bits, void* temp, cudaStream_t s, bool* in_alt) {
+    *in_alt = false;
+    if (n <= 1 || key_bits <= 0) return KNN_OK;
+    const uint32_t nblocks = (n + kSortTile - 1) / kSortTile;
+    uint32_t* counts = static_cast<uint32_t*>(temp);
+    uint32_t* offsets = counts + 256 * static_cast<size_t>(nblocks);
+    uint32_t *ki = keys, *vi = vals, *ko = keys_alt, *vo = vals_alt;
+    for (int shift = 0; shift < key_bits; shift += 8) {
+        radix_hist_kernel<<<nblocks, kSortThreads, 0, s>>>(ki, n, shift, counts, nblocks);
+        scan_rows_kernel<<<1, 1024, 0, s>>>(counts, offsets, 256 * nblocks);
+        radix_scatter_kernel<<<nblocks, kSortThreads, 0, s>>>(ki, vi, n, shift, offsets, nblocks, ko, vo);
+        KNN_LAUNCHED_N(3);
+        uint32_t* t = ki;
+        ki = ko;
+        ko = t;
+        t = vi;
+        vi = vo;
+        vo = t;
+        *in_alt = !*in_alt;
+    }
+    return KNN_OK;
+}
+
+int scan_rows_exclusive(const uint32_t* counts, uint32_t* out, uint32_t rows, uint32_t cols,
+                        cudaStream_t s) {
+    if (rows == 0 || cols == 0) return KNN_OK;
+    scan_rows_kernel<<<rows, 1024, 0, s>>>(counts, out, cols);
+    KNN_LAUNCHED();
+    return KNN_OK;
+}
+
+int fill_empty_rows(const QueryArgs& a, cudaStream_t s) {
+    const uint64_t total = static_cast<uint64_t>(a.count) * a.k;
+    if (total == 0) return KNN_OK;
+    const uint32_t blocks = static_cast<uint32_t>((total + 255) / 256);
+    fill_rows_kernel<<<blocks, 256, 0, s>>>(a.count, a.k, a.max_d2, a.radii, a.out_idx, a.out_dist);
+    KNN_LAUNCHED();
+    return KNN_OK;
+}
+
+int sm_count() {
+    static int cached = 0;
+    if (cached == 0) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cached = v > 0 ? v : 1;
+    }
+    return cached;
+}
+
+}  // namespace knn

@@ -1,0 +1,227 @@
+"""Python mirror of the reference's GPU API (namespace KnnTrees of rezvoj/CudaExactKnn).
+
+Same names, argument meanings and error behaviour, with torch CUDA tensors standing in for the
+reference's raw device pointers:
+
+    reference (src/KnnTrees.cuh, src/*Gpu.cuh)            here
+    ------------------------------------------------------------------------------------------
+    Query<Dims,K>{points, count, maxDistance2,            Query(points, count, max_distance2,
+                  rIndexes, rDistances}                         r_indexes, r_distances)
+    BruteForceGpu<Dims>(devicePoints, size)               BruteForceGpu(points, size)
+    KdTreeGpu<Dims,AuxDims,CBlockSize>(p, size, skips)    KdTreeGpu(points, size, depth_skips,
+                                                                    aux_dims, c_block_size)
+    BallTreeGpu<Dims,CBlockSize>(p, size, skips)          BallTreeGpu(points, size, depth_skips,
+                                                                      c_block_size)
+    bf.batchKnn<K,BLOCK,HEAP,SH_NN>(query)                bf.batch_knn(query, block_size, heap,
+                                                                       shmem_tracking)
+    tree.batchKnn<K,BLOCK,HEAP,SH_NN,SH_STACK>(query)     tree.batch_knn(query, block_size, heap,
+                                                                         shmem_tracking, shmem_stack)
+    KnnTrees::CudaException                               CudaException (a KnnError)
+
+K is the second dimension of r_indexes / r_distances ([count, K] int32 / float32 tensors).
+Like the reference, batch_knn waits for the work to finish (``sync=False`` leaves it enqueued on
+the current torch stream).  Results are the reference's answers with every row in ascending
+(distance, index) order.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+
+import torch
+
+from . import _lib
+from ._lib import KnnError
+
+CudaException = KnnError
+
+
+def _stream_handle(stream: torch.cuda.Stream | None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def _check_points(points: torch.Tensor, name: str = "points") -> torch.Tensor:
+    if not isinstance(points, torch.Tensor) or not points.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if points.dtype != torch.float32 or points.dim() != 2:
+        raise TypeError(f"{name} must be float32 [n, dims]")
+    return points.contiguous()
+
+
+@dataclass
+class Query:
+    """Query<Dims,K> (src/KnnTrees.cuh:224-231): device points and result buffers."""
+
+    points: torch.Tensor
+    count: int
+    max_distance2: float
+    r_indexes: torch.Tensor | None = None
+    r_distances: torch.Tensor | None = None
+
+    def ensure_outputs(self, k: int) -> None:
+        dev = self.points.device
+        if self.r_indexes is None:
+            self.r_indexes = torch.empty((self.count, k), dtype=torch.int32, device=dev)
+        if self.r_distances is None:
+            self.r_distances = torch.empty((self.count, k), dtype=torch.float32, device=dev)
+
+
+class _Index:
+    structure = -1
+
+    def __init__(self):
+        self._h = ctypes.c_void_p()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def info(self) -> _lib.IndexInfo:
+        out = _lib.IndexInfo()
+        _lib.check(_lib.load().knn_index_get_info(self._h, ctypes.byref(out)))
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            _lib.load().knn_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _query(self, query: Query, k: int | None, o: _lib.QueryOpts, sync: bool, stream, radii=None):
+        q = _check_points(query.points, "query.points")
+        if k is None:
+            if query.r_indexes is None:
+                raise ValueError("k is needed when the query has no result buffers")
+            k = int(query.r_indexes.shape[1])
+        query.ensure_outputs(k)
+        for t, dt in ((query.r_indexes, torch.int32), (query.r_distances, torch.float32)):
+            if t.dtype != dt or t.shape[0] < query.count or t.shape[1] != k or not t.is_contiguous():
+                raise TypeError("result buffers must be contiguous [count, k] int32 / float32")
+        if q.shape[0] < query.count:
+            raise ValueError("query.points has fewer rows than query.count")
+        lib = _lib.load()
+        if radii is None:
+            st = lib.knn_query(self._h, q.data_ptr(), query.count, float(query.max_distance2), k,
+                               query.r_indexes.data_ptr(), query.r_distances.data_ptr(),
+                               ctypes.byref(o), _stream_handle(stream))
+        else:
+            st = lib.knn_query_radii(self._h, q.data_ptr(), query.count, radii.data_ptr(), k,
+                                     query.r_indexes.data_ptr(), query.r_distances.data_ptr(),
+                                     ctypes.byref(o), _stream_handle(stream))
+        _lib.check(st)
+        if sync:
+            torch.cuda.synchronize(q.device)
+        return query.r_indexes, query.r_distances
+
+    def batch_knn(self, query: Query, k: int | None = None, block_size: int = 0, heap: bool = False,
+                  shmem_tracking: bool = False, shmem_stack: bool = False, flags: int = 0,
+                  leaf_scan: int = 0, sync: bool = True, stream=None):
+        """batchKnn<K,BLOCK_SIZE,USE_HEAP_TRACKING,USE_TRACKING_SHMEM,USE_STACK_SHMEM>(query)."""
+        o = _lib.opts(block_size, heap, shmem_tracking, shmem_stack, flags, leaf_scan)
+        return self._query(query, k, o, sync, stream)
+
+    def batch_knn_radii(self, query: Query, radii: torch.Tensor, k: int | None = None, sync: bool = True,
+                        stream=None, **kw):
+        """batch_knn with one max_distance2 per query (float32 CUDA tensor [count])."""
+        if radii.dtype != torch.float32 or not radii.is_cuda or radii.numel() < query.count:
+            raise TypeError("radii must be a float32 CUDA tensor with one entry per query")
+        o = _lib.opts(**{key: kw[key] for key in kw})
+        return self._query(query, k, o, sync, stream, radii=radii.contiguous())
+
+    def knn(self, queries: torch.Tensor, k: int, max_distance2: float = math.inf, **kw):
+        """Convenience: new result tensors for `queries` ([count, dims] CUDA float32)."""
+        q = Query(queries, int(queries.shape[0]), max_distance2)
+        return self.batch_knn(q, k, **kw)
+
+    def knn_host(self, queries, k: int, max_distance2: float = math.inf, out_idx=None, out_dist=None,
+                 block_size=0, heap=False, shmem_tracking=False, shmem_stack=False, flags=0, stream=None):
+        """End-to-end query on host buffers (numpy or CPU tensors; pinned memory is fastest)."""
+        qt = torch.as_tensor(queries)
+        if qt.dtype != torch.float32 or not qt.is_contiguous() or qt.is_cuda:
+            raise TypeError("host queries must be a contiguous float32 CPU array")
+        count = int(qt.shape[0])
+        if out_idx is None:
+            out_idx = torch.empty((count, k), dtype=torch.int32, pin_memory=qt.is_pinned())
+        if out_dist is None:
+            out_dist = torch.empty((count, k), dtype=torch.float32, pin_memory=qt.is_pinned())
+        o = _lib.opts(block_size, heap, shmem_tracking, shmem_stack, flags)
+        st = _lib.load().knn_query_host(self._h, qt.data_ptr(), count, float(max_distance2), k,
+                                        out_idx.data_ptr(), out_dist.data_ptr(), ctypes.byref(o),
+                                        _stream_handle(stream))
+        _lib.check(st)
+        return out_idx, out_dist
+
+    def stats(self, query: Query, k: int, **kw) -> _lib.QueryCounters:
+        """Runs the query with device counters (nodes visited, leaves, points scanned)."""
+        q = _check_points(query.points)
+        query.ensure_outputs(k)
+        o = _lib.opts(**kw)
+        out = _lib.QueryCounters()
+        st = _lib.load().knn_query_stats(self._h, q.data_ptr(), query.count, float(query.max_distance2), k,
+                                         query.r_indexes.data_ptr(), query.r_distances.data_ptr(),
+                                         ctypes.byref(o), _stream_handle(None), ctypes.byref(out))
+        _lib.check(st)
+        return out
+
+
+class BruteForceGpu(_Index):
+    """BruteForceGpu<Dims> (src/BruteForceGpu.cuh:54-85)."""
+
+    structure = _lib.BRUTE_FORCE
+
+    def __init__(self, points: torch.Tensor, size: int | None = None, stream=None):
+        super().__init__()
+        p = _check_points(points)
+        n = int(p.shape[0] if size is None else size)
+        self.dims = int(p.shape[1])
+        _lib.check(_lib.load().knn_bf_create(p.data_ptr(), n, self.dims, _stream_handle(stream),
+                                             ctypes.byref(self._h)))
+
+
+class KdTreeGpu(_Index):
+    """KdTreeGpu<Dims,AuxDims,CBlockSize> (src/KdTreeGpu.cuh:444-574)."""
+
+    structure = _lib.KD_TREE
+
+    def __init__(self, points: torch.Tensor, size: int | None = None, depth_skips: int = 0,
+                 aux_dims: int | None = None, c_block_size: int = 256, stream=None):
+        super().__init__()
+        p = _check_points(points)
+        n = int(p.shape[0] if size is None else size)
+        self.dims = int(p.shape[1])
+        aux = self.dims if aux_dims is None else int(aux_dims)
+        _lib.check(_lib.load().knn_kd_create(p.data_ptr(), n, self.dims, aux, depth_skips, c_block_size,
+                                             _stream_handle(stream), ctypes.byref(self._h)))
+
+
+class BallTreeGpu(_Index):
+    """BallTreeGpu<Dims,CBlockSize> (src/BallTreeGpu.cuh:463-650)."""
+
+    structure = _lib.BALL_TREE
+
+    def __init__(self, points: torch.Tensor, size: int | None = None, depth_skips: int = 1,
+                 c_block_size: int = 256, stream=None):
+        super().__init__()
+        p = _check_points(points)
+        n = int(p.shape[0] if size is None else size)
+        self.dims = int(p.shape[1])
+        _lib.check(_lib.load().knn_ball_create(p.data_ptr(), n, self.dims, depth_skips, c_block_size,
+                                               _stream_handle(stream), ctypes.byref(self._h)))
+
+
+def build_index(structure: str, points: torch.Tensor, depth_skips: int | None = None, **kw) -> _Index:
+    if structure == "bf":
+        return BruteForceGpu(points, **kw)
+    if structure == "kd":
+        return KdTreeGpu(points, depth_skips=0 if depth_skips is None else depth_skips, **kw)
+    if structure == "ball":
+        return BallTreeGpu(points, depth_skips=1 if depth_skips is None else depth_skips, **kw)
+    raise ValueError(structure)

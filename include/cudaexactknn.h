@@ -1,0 +1,171 @@
+/*
+ * cudaexactknn.h -- C ABI of the GB300 (sm_103a) exact k-nearest-neighbour engine.
+ *
+ * Plain pointers and sizes only; every function returns a knn_status code and never throws.
+ * knn_last_error() gives a human-readable message for the calling thread's last failure.
+ *
+ * The entry points replace the GPU classes of the reference header library (namespace
+ * KnnTrees of rezvoj/CudaExactKnn):
+ *
+ *   knn_bf_create    BruteForceGpu<Dims>::BruteForceGpu(devicePoints, n)      src/BruteForceGpu.cuh:63-68
+ *   knn_kd_create    KdTreeGpu<Dims,AuxDims,CBlockSize>::KdTreeGpu(p,n,skips) src/KdTreeGpu.cuh:375-385
+ *   knn_ball_create  BallTreeGpu<Dims,CBlockSize>::BallTreeGpu(p,n,skips)     src/BallTreeGpu.cuh:614-624
+ *   knn_destroy      the three destructors                                     src/BruteForceGpu.cuh:70-72,
+ *                                                                             src/KdTreeGpu.cuh:387-390,
+ *                                                                             src/BallTreeGpu.cuh:626-629
+ *   knn_query        batchKnn<K,BLOCK_SIZE,HEAP,SH_NN[,SH_STACK]>(Query&)      src/BruteForceGpu.cuh:74-83,
+ *                                                                             src/KdTreeGpu.cuh:393-410,
+ *                                                                             src/BallTreeGpu.cuh:631-648
+ *                    with Query<Dims,K> = {points, count, maxDistance2,        src/KnnTrees.cuh:224-231
+ *                                          rIndexes, rDistances}
+ *   knn_status_string / knn_last_error   KnnTrees::CudaException's message     src/KnnTrees.cuh:20-23
+ *
+ * Semantics kept from the reference:
+ *   - points are float32 [n][dims] row-major (Array<float,Dims>), device memory;
+ *   - results are int32 [count][k] indices and float32 [count][k] squared distances;
+ *   - a slot is filled by the k smallest keys (bits(dist2) << 32 | uint32(index)) with
+ *     dist2 <= max_distance2; unfilled slots hold index -1 and distance max_distance2;
+ *   - depthSkips: leaves of 2^skips points, skips clamped to log2Ceil(n)-1, and >= 1 for the
+ *     ball tree; k-d split dimension = depth % aux_dims.
+ * Differences, by design:
+ *   - rows are always in ascending key order (the reference's heap tracking leaves heap order);
+ *   - trees prune on bound > k-th distance with rigorous rounding margins, so every structure
+ *     returns exactly brute force's answer, ties included;
+ *   - work is enqueued on the caller's stream and the call returns without synchronising
+ *     unless KNN_QF_SYNC is set (the reference synchronises the whole device per call);
+ *   - a negative or NaN max_distance2, k == 0 or dims == 0 is KNN_ERR_INVALID_ARGUMENT.
+ *
+ * Supported sizes: 1 <= dims <= 128, 1 <= k <= 128, n < 2^31, count < 2^31.
+ * One query at a time per index: an index owns one scratch workspace.
+ */
+#ifndef CUDAEXACTKNN_H
+#define CUDAEXACTKNN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define KNN_API __attribute__((visibility("default")))
+#else
+#define KNN_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct knn_index knn_index;
+
+typedef enum knn_status {
+    KNN_OK = 0,
+    KNN_ERR_INVALID_ARGUMENT = 1,
+    KNN_ERR_UNSUPPORTED = 2,   /* dims or k outside the supported range */
+    KNN_ERR_CUDA = 3,          /* a CUDA runtime call failed (message in knn_last_error) */
+    KNN_ERR_OUT_OF_MEMORY = 4,
+    KNN_ERR_DEVICE_LIMIT = 5,  /* a kernel's bounds check fired; results are not valid */
+    KNN_ERR_NOT_TRAINED = 6    /* KNN_QF_LEARNED_RADIUS without a trained radius model */
+} knn_status;
+
+typedef enum knn_structure {
+    KNN_BRUTE_FORCE = 0,
+    KNN_KD_TREE = 1,
+    KNN_BALL_TREE = 2
+} knn_structure;
+
+/* Query flags. */
+#define KNN_QF_SYNC 1u           /* synchronise the stream before returning */
+#define KNN_QF_AUTOTUNE 2u       /* engine picks block size, tracking, storage and leaf size */
+#define KNN_QF_LEARNED_RADIUS 4u /* seed each query's radius from the trained model; queries
+                                    with fewer than k hits are re-run unbounded */
+#define KNN_QF_BF16_FILTER 8u    /* brute force, dims >= 16: BF16 tensor-core filter + FP32 rescore */
+#define KNN_QF_KEEP_ORDER 16u    /* do not reorder queries for locality */
+#define KNN_QF_TIMING 32u        /* record CUDA events around the query and its search kernel */
+
+/*
+ * Run-time form of batchKnn's template arguments (src/KdTreeGpu.cuh:392,
+ * src/BruteForceGpu.cuh:74): BLOCK_SIZE, USE_HEAP_TRACKING, USE_TRACKING_SHMEM,
+ * USE_STACK_SHMEM.  A zeroed struct (or NULL) means block 0 = engine default, sorted
+ * insertion tracking in registers, stack in registers.
+ */
+typedef struct knn_query_opts {
+    uint32_t block_size;
+    uint32_t heap_tracking;
+    uint32_t shmem_tracking;
+    uint32_t shmem_stack;
+    uint32_t flags;
+    uint32_t leaf_scan;     /* trees: scan whole subtrees of at most this many points as one
+                               leaf (0 = the tree's own leaves) */
+    uint32_t reserved[2];
+} knn_query_opts;
+
+/* Per-query statistics written by knn_query_stats (summed over the batch). */
+typedef struct knn_query_counters {
+    uint64_t nodes_visited;    /* internal nodes whose bound was evaluated */
+    uint64_t leaves_visited;   /* leaves scanned */
+    uint64_t points_scanned;   /* leaf slots whose distance was computed */
+    uint64_t fallback_queries; /* learned-radius queries re-run unbounded */
+    uint64_t reserved[4];
+} knn_query_counters;
+
+typedef struct knn_index_info {
+    uint32_t structure;   /* knn_structure */
+    uint32_t n;
+    uint32_t dims;
+    uint32_t aux_dims;    /* k-d split dimensions (k-d tree), else dims */
+    uint32_t depth_skips; /* after clamping */
+    uint32_t node_depth;  /* internal node levels */
+    uint32_t leaf_slots;  /* 2^depth_skips */
+    uint32_t node_count;  /* internal nodes, 2^node_depth - 1 */
+    uint64_t device_bytes;
+    float build_ms;       /* device time of the construction, CUDA events */
+    uint32_t radius_model;/* 1 when a learned radius model is attached */
+} knn_index_info;
+
+/* ---- construction (points: device pointer, float32 [n][dims]; read during the call only) --- */
+KNN_API int knn_bf_create(const float* d_points, uint32_t n, uint32_t dims, void* stream,
+                  knn_index** out);
+KNN_API int knn_kd_create(const float* d_points, uint32_t n, uint32_t dims, uint32_t aux_dims,
+                  uint32_t depth_skips, uint32_t build_block, void* stream, knn_index** out);
+KNN_API int knn_ball_create(const float* d_points, uint32_t n, uint32_t dims, uint32_t depth_skips,
+                    uint32_t build_block, void* stream, knn_index** out);
+KNN_API int knn_destroy(knn_index* index);
+KNN_API int knn_index_get_info(const knn_index* index, knn_index_info* out);
+
+/* ---- queries (device pointers; enqueued on `stream`, a cudaStream_t, NULL = legacy stream) -- */
+KNN_API int knn_query(knn_index* index, const float* d_queries, uint32_t count, float max_distance2,
+              uint32_t k, int32_t* d_indexes, float* d_distances, const knn_query_opts* opts,
+              void* stream);
+
+/* As knn_query, with one max_distance2 per query (device float32 [count]). */
+KNN_API int knn_query_radii(knn_index* index, const float* d_queries, uint32_t count,
+                    const float* d_max_distance2, uint32_t k, int32_t* d_indexes,
+                    float* d_distances, const knn_query_opts* opts, void* stream);
+
+/* As knn_query with HOST buffers: copies queries in and results out on `stream` and
+ * synchronises.  Pinned host memory gives full-speed copies. */
+KNN_API int knn_query_host(knn_index* index, const float* h_queries, uint32_t count,
+                   float max_distance2, uint32_t k, int32_t* h_indexes, float* h_distances,
+                   const knn_query_opts* opts, void* stream);
+
+/* Runs the query with device counters enabled and returns the summed counters (synchronous). */
+KNN_API int knn_query_stats(knn_index* index, const float* d_queries, uint32_t count,
+                    float max_distance2, uint32_t k, int32_t* d_indexes, float* d_distances,
+                    const knn_query_opts* opts, void* stream, knn_query_counters* out);
+
+/* Device time (ms) of the index's last KNN_QF_TIMING query: the whole query and its main search
+ * kernel alone (CUDA events on the query's stream; waits for the query to finish). */
+KNN_API int knn_last_query_timing(knn_index* index, float* total_ms, float* kernel_ms);
+
+/* Number of kernels this library has launched since it was loaded (all indexes, all threads). */
+KNN_API uint64_t knn_launch_count(void);
+
+/* ---- errors ------------------------------------------------------------------------------ */
+KNN_API const char* knn_status_string(int status);
+KNN_API const char* knn_last_error(void);
+KNN_API int knn_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUDAEXACTKNN_H */

@@ -1,0 +1,76 @@
+"""C-ABI checks that need no GPU: the library loads, exports what the header declares, and
+rejects bad arguments before touching the device."""
+
+import ctypes
+import os
+import subprocess
+
+import pytest
+
+from cudaexactknn_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    lib = _lib.load()
+    declared = _lib.header_symbols()
+    assert len(declared) >= 12
+    for name in declared:
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert set(declared) <= exported
+
+
+def test_library_is_built_for_sm_103a():
+    out = subprocess.run(["cuobjdump", "--list-elf", _lib.LIB_PATH], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+def test_status_strings_and_version():
+    lib = _lib.load()
+    assert lib.knn_status_string(0) == b"ok"
+    assert lib.knn_status_string(_lib.ERR_INVALID_ARGUMENT) == b"invalid argument"
+    assert lib.knn_version() >= 10000
+
+
+@pytest.mark.parametrize("dims,expect", [(0, _lib.ERR_INVALID_ARGUMENT), (129, _lib.ERR_UNSUPPORTED)])
+def test_create_rejects_bad_dims_without_a_device(dims, expect):
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    st = lib.knn_bf_create(None, 10, dims, None, ctypes.byref(h))
+    assert st == expect
+    assert not h
+    assert lib.knn_last_error()
+
+
+def test_create_rejects_null_points_and_bad_aux_dims():
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    assert lib.knn_kd_create(None, 10, 3, 3, 0, 256, None, ctypes.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    assert lib.knn_kd_create(ctypes.c_void_p(16), 10, 3, 4, 0, 256, None, ctypes.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    assert lib.knn_kd_create(ctypes.c_void_p(16), 10, 3, 0, 0, 256, None, ctypes.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    assert lib.knn_ball_create(None, 10, 3, 1, 256, None, None) == _lib.ERR_INVALID_ARGUMENT
+
+
+def test_query_rejects_null_index_and_bad_k():
+    lib = _lib.load()
+    o = _lib.opts()
+    assert lib.knn_query(None, None, 1, 1.0, 4, None, None, ctypes.byref(o), None) == _lib.ERR_INVALID_ARGUMENT
+
+
+def test_cpp_shim_headers_compile():
+    """The C++ KnnTrees drop-in headers compile (host code, no GPU needed)."""
+    src = os.path.join(ROOT, "tests", "cpp", "shim_compile_check.cu")
+    if not os.path.exists(src):
+        pytest.skip("shim check source missing")
+    out = os.path.join(ROOT, "cudaexactknn_gb300", "_build", "shim_compile_check.o")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    r = subprocess.run(["nvcc", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a",
+                        f"-I{os.path.join(ROOT, 'include')}", "-c", src, "-o", out],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
