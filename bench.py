@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (debug only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-once", action="store_true",
+                    help="build the index, run one chosen-form query and exit (for ncu captures)")
     return ap.parse_args()
 
 
@@ -259,6 +261,7 @@ def main():
         run_reference(args, world, rank)
         return
 
+    import ctypes
     import torch
     from cudaexactknn_gb300 import _lib, knn
     import oracle
@@ -279,8 +282,24 @@ def main():
     query = knn.Query(qs, count, w.max_dist2, out_i, out_d)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    plain_kw = dict(block_size=32 if w.structure != "ball" else 16, heap=w.heap)
-    chosen_kw = dict(block_size=128, heap=False)
+    # Plain form: the reference benchmarks' template choices (kd <K,32,false,false,true>,
+    # ball <K,16,true,true,true>, brute force <K,32,false,false>; tests/Dim3SpeedTests.cu:38,43,
+    # tests/DimXSpeedTests.cu:52), no autotune, no learned radius.
+    plain_kw = {"kd": dict(block_size=32, shmem_stack=True), "ball": dict(block_size=16, heap=True,
+                shmem_tracking=True, shmem_stack=True), "bf": dict(block_size=32)}[w.structure]
+    # Chosen form: the engine's autotuned plan seeded by the learned radius.
+    train = w.extra.get("train")
+    report = None
+    if train is not None:
+        report = index.train_radius_model(torch.from_numpy(train).to(dev), k)
+        chosen_kw = dict(flags=_lib.QF_AUTOTUNE | _lib.QF_LEARNED_RADIUS)
+    else:
+        chosen_kw = dict(flags=_lib.QF_AUTOTUNE)
+    if args.profile_once:
+        index.batch_knn(query, k, **chosen_kw)
+        torch.cuda.synchronize(dev)
+        index.close()
+        return
 
     def timed(kw, steps, warmup):
         for _ in range(warmup):
@@ -293,7 +312,9 @@ def main():
         for s in range(steps):
             flush.zero_()
             ev[s][0].record(stream)
-            index.batch_knn(query, k, sync=False, flags=_lib.QF_TIMING, **kw)
+            timed_kw = dict(kw)
+            timed_kw["flags"] = timed_kw.get("flags", 0) | _lib.QF_TIMING
+            index.batch_knn(query, k, sync=False, **timed_kw)
             ev[s][1].record(stream)
             tot = ctypes_float()
             ker = ctypes_float()
@@ -305,7 +326,6 @@ def main():
         total_ms = sum(a.elapsed_time(b) for a, b in ev)
         return total_ms, float(np.mean(kern_ms)), launches
 
-    import ctypes
     ctypes_float = ctypes.c_float
 
     # Exactness of both forms on a sample, checked against the CPU oracle (outside timing).
@@ -320,6 +340,14 @@ def main():
 
     counters = index.stats(query, k, **plain_kw)
     alg_bytes, floor_bytes = algorithmic_bytes(w, counters, count)
+    chosen_counters = index.stats(query, k, **chosen_kw)
+    tuned = _lib.QueryOpts()
+    tuned_ms = ctypes.c_float()
+    learned = bool(chosen_kw.get("flags", 0) & _lib.QF_LEARNED_RADIUS)
+    _lib.check(lib.knn_tuned_plan(index.handle, k, int(learned), ctypes.byref(tuned), ctypes.byref(tuned_ms)))
+    tuned_plan = dict(block_size=tuned.block_size, heap=bool(tuned.heap_tracking),
+                      shmem_tracking=bool(tuned.shmem_tracking), shmem_stack=bool(tuned.shmem_stack),
+                      leaf_scan=tuned.leaf_scan, candidates_timed=tuned.reserved[0])
 
     with ClockSampler(local) as clocks:
         chosen_ms, chosen_kern_ms, launches = timed(chosen_kw, args.steps, args.warmup)
@@ -363,8 +391,16 @@ def main():
         "exact_match": {"chosen": exact["chosen"], "plain": exact["plain"], "e2e": e2e_exact,
                         "sample_queries": int(len(sample))},
         "plain": {"value": plain_qps, "ms_per_step": plain_ms / args.steps, "plan": plain_kw,
-                  "kernel_ms": plain_kern_ms},
-        "chosen": {"plan": chosen_kw, "kernel_ms": chosen_kern_ms, "speedup_vs_plain": value / plain_qps},
+                  "kernel_ms": plain_kern_ms, "roofline_frac": alg_bytes / (plain_kern_ms / 1e3) / 1e9 / peaks()[0]},
+        "chosen": {"form": "autotune + learned radius" if learned else "autotune", "plan": tuned_plan,
+                   "kernel_ms": chosen_kern_ms, "speedup_vs_plain": value / plain_qps,
+                   "fallback_queries": int(chosen_counters.fallback_queries),
+                   "visits": {"nodes": int(chosen_counters.nodes_visited),
+                              "leaves": int(chosen_counters.leaves_visited),
+                              "points": int(chosen_counters.points_scanned)},
+                   "radius_model": None if report is None else {
+                       "train_ms": report.train_ms, "samples": report.samples, "steps": report.steps,
+                       "rmse_log_kth": report.rmse, "margin": report.margin, "coverage": report.coverage}},
         "build_ms": build_ms,
         "e2e": {"value": e2e_qps, "unit": "queries/s",
                 "h2d_bytes_per_step": int(w.queries.nbytes),

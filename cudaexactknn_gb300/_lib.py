@@ -55,6 +55,17 @@ class IndexInfo(ctypes.Structure):
                 ("build_ms", ctypes.c_float), ("radius_model", ctypes.c_uint32)]
 
 
+class TrainOpts(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_uint32), ("batch", ctypes.c_uint32), ("lr", ctypes.c_float),
+                ("coverage", ctypes.c_float), ("seed", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 3)]
+
+
+class TrainReport(ctypes.Structure):
+    _fields_ = [("train_ms", ctypes.c_float), ("final_batch_loss", ctypes.c_float), ("rmse", ctypes.c_float),
+                ("margin", ctypes.c_float), ("coverage", ctypes.c_float), ("samples", ctypes.c_uint32),
+                ("steps", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
 class KnnError(RuntimeError):
     """A non-zero knn_status; ``.status`` holds the code (the reference throws CudaException)."""
 
@@ -79,8 +90,15 @@ _SIGNATURES = {
     "knn_query_host": [_vp, _vp, _u32, _f, _u32, _vp, _vp, ctypes.POINTER(QueryOpts), _vp],
     "knn_query_stats": [_vp, _vp, _u32, _f, _u32, _vp, _vp, ctypes.POINTER(QueryOpts), _vp,
                         ctypes.POINTER(QueryCounters)],
+    "knn_radius_model_train": [_vp, _vp, _u32, _u32, ctypes.POINTER(TrainOpts), _vp, ctypes.POINTER(TrainReport)],
+    "knn_radius_model_predict": [_vp, _vp, _u32, _vp, _vp],
+    "knn_radius_model_size": [_u32],
+    "knn_radius_model_export": [_vp, _vp, _u32],
+    "knn_radius_model_import": [_vp, _vp, _u32, _u32],
+    "knn_radius_model_gradients": [_vp, _u32, _vp, _vp, _u32, _vp, _vp],
     "knn_last_query_timing": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
     "knn_launch_count": [],
+    "knn_tuned_plan": [_vp, _u32, _u32, ctypes.POINTER(QueryOpts), ctypes.POINTER(ctypes.c_float)],
     "knn_status_string": [ctypes.c_int],
     "knn_last_error": [],
     "knn_version": [],
@@ -92,7 +110,7 @@ _lib = None
 def header_symbols() -> list[str]:
     """Names of the functions include/cudaexactknn.h declares."""
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"KNN_API\s+(?:const\s+char\s*\*|int|uint64_t)\s+(knn_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"KNN_API\s+(?:const\s+char\s*\*|int|uint64_t|uint32_t)\s+(knn_\w+)\s*\(", text)))
 
 
 def load() -> ctypes.CDLL:
@@ -109,6 +127,8 @@ def load() -> ctypes.CDLL:
             fn.restype = ctypes.c_char_p
         elif name == "knn_launch_count":
             fn.restype = ctypes.c_uint64
+        elif name == "knn_radius_model_size":
+            fn.restype = ctypes.c_uint32
         else:
             fn.restype = ctypes.c_int
     _lib = lib

@@ -25,12 +25,15 @@ struct BallParams {
     const float* leaf;
     uint32_t leaf_stride;
     uint32_t node_count;
+    uint32_t node_depth;
+    uint32_t stop_depth;
     uint32_t leaf_slots;
     float margin;
     const float* queries;
     uint32_t dims;
     uint32_t nq;
     const uint32_t* order;
+    const uint32_t* count_dev;
     float max_d2;
     const float* radii;
     uint32_t k;
@@ -63,7 +66,7 @@ template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
 __global__ void __launch_bounds__(256) ball_knn_kernel(const BallParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.nq) return;  // no block-wide barriers below
+    if (t >= (p.count_dev ? *p.count_dev : p.nq)) return;  // no block-wide barriers below
     uint64_t* sh_nn = reinterpret_cast<uint64_t*>(smem);
     uint32_t* sh_st = reinterpret_cast<uint32_t*>(smem + tracker_smem_bytes(SHNN, KMAX, blockDim.x));
 
@@ -86,7 +89,8 @@ __global__ void __launch_bounds__(256) ball_knn_kernel(const BallParams p) {
         st.pop(&node, &bound);
         if (bound > tr.radius()) continue;
         bool pruned = false;
-        while (node < p.node_count) {
+        uint32_t depth = heap_depth(node);
+        while (depth < p.stop_depth) {
             const uint32_t l = 2 * node + 1;
             float rl, rr;
             const float sl = centre_dist<DP>(q, p.ball + static_cast<size_t>(l) * p.ball_stride, &rl);
@@ -104,6 +108,7 @@ __global__ void __launch_bounds__(256) ball_knn_kernel(const BallParams p) {
                 // order above is approximate, so it is checked on its own.
                 if (far_b <= tr.radius()) {
                     node = left_first ? l + 1 : l;
+                    ++depth;
                     continue;
                 }
                 pruned = true;
@@ -111,14 +116,16 @@ __global__ void __launch_bounds__(256) ball_knn_kernel(const BallParams p) {
             }
             if (far_b <= tr.radius()) overflow |= !st.push(left_first ? l + 1 : l, far_b);
             node = close_child;
+            ++depth;
         }
         if (pruned) continue;
-        const float* slot = p.leaf + static_cast<size_t>(node - p.node_count) * p.leaf_slots * p.leaf_stride;
+        const SlotRange r = subtree_slots(node, depth, p.node_depth, p.node_count, p.leaf_slots);
+        const float* slot = p.leaf + r.first * p.leaf_stride;
         ++lc.leaves;
-        for (uint32_t s = 0; s < p.leaf_slots; ++s, slot += p.leaf_stride) {
+        for (uint32_t s = 0; s < r.count; ++s, slot += p.leaf_stride) {
             int32_t id;
             const float d2 = slot_dist<DP>(q, slot, &id);
-            if (id < 0) break;
+            if (id < 0) continue;
             ++lc.points;
             tr.offer(make_key(d2, id));
         }
@@ -165,12 +172,15 @@ static int launch_ball(knn_index* ix, const QueryArgs& a, const QueryPlan& plan,
     p.leaf = ix->leaf.as<float>();
     p.leaf_stride = ix->leaf_stride;
     p.node_count = ix->node_count;
+    p.node_depth = ix->node_depth;
+    p.stop_depth = scan_depth_for(ix->node_depth, ix->leaf_slots, plan.leaf_scan);
     p.leaf_slots = ix->leaf_slots;
     p.margin = rel_margin(ix->dims);
     p.queries = a.queries;
     p.dims = ix->dims;
     p.nq = a.count;
     p.order = order;
+    p.count_dev = a.count_dev;
     p.max_d2 = a.max_d2;
     p.radii = a.radii;
     p.k = a.k;
@@ -204,9 +214,9 @@ static int launch_ball_variant(knn_index* ix, const QueryArgs& a, const QueryPla
 
 template <uint32_t DP>
 int ball_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s) {
-    const uint32_t* order = nullptr;
+    const uint32_t* order = a.order;
     const uint32_t levels = std::min<uint32_t>(ix->node_depth, 24);
-    if (p.reorder && a.count >= 4096 && levels > 0) {
+    if (!order && p.reorder && a.count >= 4096 && levels > 0) {
         const size_t nq = a.count;
         const size_t need = carve_bytes({nq * 4, nq * 4, nq * 4, nq * 4, radix_sort_temp_bytes(a.count)});
         KNN_TRY(ix->workspace.reserve(need));

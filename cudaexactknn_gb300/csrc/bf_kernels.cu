@@ -29,6 +29,8 @@ struct BfParams {
     uint32_t nq;
     float max_d2;
     const float* radii;
+    const uint32_t* order;      // thread -> query, or null
+    const uint32_t* count_dev;  // live thread count on the device, or null
     uint32_t k;
     uint32_t chunk;  // points per split
     uint32_t tile;   // points per shared-memory tile
@@ -45,12 +47,13 @@ __global__ void __launch_bounds__(256) bf_knn_kernel(const BfParams p) {
     uint64_t* sh_nn = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(p.tile) * PS * sizeof(float));
 
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = t < p.nq;
+    const bool active = t < (p.count_dev ? *p.count_dev : p.nq);
+    const uint32_t qi = active ? (p.order ? p.order[t] : t) : 0u;
     float q[PS];
 #pragma unroll
     for (int d = 0; d < PS; ++d)
-        q[d] = (active && static_cast<uint32_t>(d) < p.dims) ? p.queries[static_cast<size_t>(t) * p.dims + d] : 0.0f;
-    const float r2 = active ? (p.radii ? p.radii[t] : p.max_d2) : 0.0f;
+        q[d] = (active && static_cast<uint32_t>(d) < p.dims) ? p.queries[static_cast<size_t>(qi) * p.dims + d] : 0.0f;
+    const float r2 = active ? (p.radii ? p.radii[qi] : p.max_d2) : 0.0f;
 
     Tracker<KMAX, HEAP, SHNN> tr;
     tr.init(p.k, r2, sh_nn + threadIdx.x, blockDim.x);
@@ -80,7 +83,7 @@ __global__ void __launch_bounds__(256) bf_knn_kernel(const BfParams p) {
     if (p.partial)
         tr.emit_keys(p.k, p.partial + (static_cast<size_t>(blockIdx.y) * p.nq + t) * p.k);
     else
-        tr.emit(p.k, p.out_idx + static_cast<size_t>(t) * p.k, p.out_dist + static_cast<size_t>(t) * p.k);
+        tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
 }
 
 // Combines the per-split sorted key lists of each query into its final row.
@@ -88,18 +91,21 @@ template <int KMAX>
 __global__ void __launch_bounds__(128) bf_merge_kernel(const uint64_t* __restrict__ partial, uint32_t splits,
                                                        uint32_t nq, uint32_t k, float max_d2,
                                                        const float* __restrict__ radii,
+                                                       const uint32_t* __restrict__ order,
+                                                       const uint32_t* __restrict__ count_dev,
                                                        int32_t* __restrict__ out_idx,
                                                        float* __restrict__ out_dist) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nq) return;
+    if (t >= (count_dev ? *count_dev : nq)) return;
+    const uint32_t qi = order ? order[t] : t;
     Tracker<KMAX, false, false> tr;
-    tr.init(k, radii ? radii[t] : max_d2, nullptr, 0);
+    tr.init(k, radii ? radii[qi] : max_d2, nullptr, 0);
     for (uint32_t s = 0; s < splits; ++s) {
         const uint64_t* row = partial + (static_cast<size_t>(s) * nq + t) * k;
         for (uint32_t i = 0; i < k; ++i)
             if (!tr.offer(row[i])) break;  // rows are ascending
     }
-    tr.emit(k, out_idx + static_cast<size_t>(t) * k, out_dist + static_cast<size_t>(t) * k);
+    tr.emit(k, out_idx + static_cast<size_t>(qi) * k, out_dist + static_cast<size_t>(qi) * k);
 }
 
 template <int DP, int KMAX, bool HEAP, bool SHNN>
@@ -131,6 +137,8 @@ static int launch_bf(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, c
     p.nq = a.count;
     p.max_d2 = a.max_d2;
     p.radii = a.radii;
+    p.order = a.order;
+    p.count_dev = a.count_dev;
     p.k = a.k;
     p.chunk = chunk;
     p.tile = tile;
@@ -148,7 +156,8 @@ static int launch_bf(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, c
     if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
     if (splits > 1) {
         bf_merge_kernel<KMAX><<<ceil_div(a.count, 128), 128, 0, s>>>(p.partial, splits, a.count, a.k, a.max_d2,
-                                                                      a.radii, a.out_idx, a.out_dist);
+                                                                      a.radii, a.order, a.count_dev, a.out_idx,
+                                                                      a.out_dist);
         KNN_LAUNCHED();
     }
     return KNN_OK;

@@ -4,8 +4,11 @@
 
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <new>
+#include <vector>
 
 #include "knn_internal.h"
 
@@ -113,6 +116,131 @@ int make_plan(const knn_index* ix, const knn_query_opts* o, knn::QueryPlan* p) {
     return KNN_OK;
 }
 
+int dispatch(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& plan, cudaStream_t s) {
+    if (ix->n == 0) return knn::fill_empty_rows(a, s);
+    switch (ix->structure) {
+        case KNN_BRUTE_FORCE: return knn::bf_query(ix, a, plan, s);
+        case KNN_KD_TREE: return knn::kd_query(ix, a, plan, s);
+        case KNN_BALL_TREE: return knn::ball_query(ix, a, plan, s);
+        default: return fail(KNN_ERR_INVALID_ARGUMENT, "unknown structure");
+    }
+}
+
+// Learned radius: seed each query's radius from the model, search, collect the queries that
+// found fewer than k points inside a seed below the caller's radius, and search those again
+// with the caller's radius.  Results are exact either way.
+int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& plan, cudaStream_t s) {
+    const size_t n = a.count;
+    KNN_TRY(ix->seed_ws.reserve(knn::carve_bytes({n * 4, n * 4, 256})));
+    knn::Carver c(ix->seed_ws.ptr);
+    float* radii = c.take<float>(n);
+    uint32_t* list = c.take<uint32_t>(n);
+    uint32_t* list_count = c.take<uint32_t>(1);
+    KNN_TRY(knn::model_predict(ix->model.as<float>(), ix->dims, a.queries, a.count, a.max_d2, a.radii, radii,
+                               nullptr, s));
+    knn::QueryArgs seeded = a;
+    seeded.radii = radii;
+    KNN_TRY(dispatch(ix, seeded, plan, s));
+    KNN_TRY(knn::model_fallbacks(a.out_idx, a.count, a.k, radii, a.max_d2, a.radii, list, list_count, a.counters, s));
+    knn::QueryArgs again = a;
+    again.order = list;
+    again.count_dev = list_count;
+    knn::QueryPlan plain = plan;
+    plain.timing = false;  // the timed kernel span stays the seeded search
+    return dispatch(ix, again, plain, s);
+}
+
+int k_slot(uint32_t k) {
+    switch (knn::k_class(k)) {
+        case 8: return 0;
+        case 16: return 1;
+        case 32: return 2;
+        case 64: return 3;
+        default: return 4;
+    }
+}
+
+// Picks the fastest plan for this index and k by timing candidates on up to 32768 of the
+// caller's queries (CUDA events, best of two runs each), in three stages: leaf bucket size,
+// then block size, then tracker/stack storage.  Results are exact for every candidate.
+int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t s, knn::QueryPlan* out,
+             float* best_ms, uint32_t* tried) {
+    knn::QueryArgs t = a;
+    t.count = std::min<uint32_t>(a.count, 32768);
+    t.counters = nullptr;
+    cudaEvent_t e0, e1;
+    KNN_TRY_CUDA(cudaEventCreate(&e0));
+    KNN_TRY_CUDA(cudaEventCreate(&e1));
+    int rc = KNN_OK;
+    uint32_t n_tried = 0;
+    auto time_plan = [&](const knn::QueryPlan& p, float* ms) -> int {
+        float best = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+            KNN_TRY_CUDA(cudaEventRecord(e0, s));
+            KNN_TRY(learned ? seeded_query(ix, t, p, s) : dispatch(ix, t, p, s));
+            KNN_TRY_CUDA(cudaEventRecord(e1, s));
+            KNN_TRY_CUDA(cudaEventSynchronize(e1));
+            float v = 0.0f;
+            KNN_TRY_CUDA(cudaEventElapsedTime(&v, e0, e1));
+            if (rep > 0) best = std::min(best, v);  // the first run warms caches and workspaces
+        }
+        *ms = best;
+        ++n_tried;
+        return KNN_OK;
+    };
+    knn::QueryPlan best;
+    best.block = 128;
+    float best_t = 1e30f;
+    auto consider = [&](const knn::QueryPlan& p) -> int {
+        float v = 0.0f;
+        const int r = time_plan(p, &v);
+        if (r == KNN_ERR_INVALID_ARGUMENT) return KNN_OK;  // a launch shape that does not fit: skip
+        if (r != KNN_OK) return r;
+        if (v < best_t) {
+            best_t = v;
+            best = p;
+        }
+        return KNN_OK;
+    };
+    do {
+        if (ix->structure != KNN_BRUTE_FORCE) {
+            for (uint32_t leaf : {0u, 4u, 8u, 16u, 32u, 64u}) {
+                if (leaf && leaf <= ix->leaf_slots) continue;
+                knn::QueryPlan p = best;
+                p.leaf_scan = leaf;
+                if ((rc = consider(p)) != KNN_OK) break;
+            }
+            if (rc != KNN_OK) break;
+        } else if ((rc = consider(best)) != KNN_OK) {
+            break;
+        }
+        const knn::QueryPlan stage2 = best;
+        for (uint32_t block : {32u, 64u, 256u}) {
+            knn::QueryPlan p = stage2;
+            p.block = block;
+            if ((rc = consider(p)) != KNN_OK) break;
+        }
+        if (rc != KNN_OK) break;
+        const knn::QueryPlan stage3 = best;
+        for (int v = 1; v < 8; ++v) {
+            knn::QueryPlan p = stage3;
+            p.heap = v & 1;
+            p.sh_nn = (v >> 1) & 1;
+            p.sh_stack = (v >> 2) & 1;
+            if (ix->structure == KNN_BRUTE_FORCE && p.sh_stack) continue;
+            if ((rc = consider(p)) != KNN_OK) break;
+        }
+    } while (false);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != KNN_OK) return rc;
+    best.timing = false;
+    *out = best;
+    *best_ms = best_t;
+    *tried = n_tried;
+    return KNN_OK;
+}
+
 int run_query(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts, cudaStream_t s) {
     if (!ix) return fail(KNN_ERR_INVALID_ARGUMENT, "index is null");
     if (a.k == 0) return fail(KNN_ERR_INVALID_ARGUMENT, "k must be >= 1");
@@ -127,6 +255,18 @@ int run_query(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts
     }
     knn::QueryPlan plan;
     KNN_TRY(make_plan(ix, opts, &plan));
+    const bool learned = (flags & KNN_QF_LEARNED_RADIUS) != 0;
+    if ((flags & KNN_QF_AUTOTUNE) && ix->n > 0) {
+        auto& slot = ix->tuned[k_slot(a.k)][learned ? 1 : 0];
+        if (!slot.valid) {
+            KNN_TRY(autotune(ix, a, learned, s, &slot.plan, &slot.ms, &slot.candidates));
+            slot.valid = true;
+        }
+        const bool timing = plan.timing;
+        plan = slot.plan;
+        plan.timing = timing;
+        plan.reorder = plan.reorder && (flags & KNN_QF_KEEP_ORDER) == 0;
+    }
     if (plan.timing) {
         KNN_TRY(ix->timing.ensure());
         ix->timing.valid = false;
@@ -134,17 +274,7 @@ int run_query(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts
         KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));  // empty kernel span if none runs
         KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
     }
-    int rc;
-    if (ix->n == 0) {
-        rc = knn::fill_empty_rows(a, s);
-    } else {
-        switch (ix->structure) {
-            case KNN_BRUTE_FORCE: rc = knn::bf_query(ix, a, plan, s); break;
-            case KNN_KD_TREE: rc = knn::kd_query(ix, a, plan, s); break;
-            case KNN_BALL_TREE: rc = knn::ball_query(ix, a, plan, s); break;
-            default: rc = fail(KNN_ERR_INVALID_ARGUMENT, "unknown structure"); break;
-        }
-    }
+    const int rc = learned && ix->n > 0 ? seeded_query(ix, a, plan, s) : dispatch(ix, a, plan, s);
     if (rc != KNN_OK) return rc;
     if (plan.timing) {
         KNN_TRY_CUDA(cudaEventRecord(ix->timing.total1, s));
@@ -306,7 +436,101 @@ int knn_last_query_timing(knn_index* index, float* total_ms, float* kernel_ms) {
     return KNN_OK;
 }
 
+int knn_tuned_plan(const knn_index* index, uint32_t k, uint32_t learned_radius, knn_query_opts* out, float* ms) {
+    if (!index || !out) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
+    if (k == 0 || k > knn::kMaxK) return fail(KNN_ERR_INVALID_ARGUMENT, "k %u", k);
+    const auto& slot = index->tuned[k_slot(k)][learned_radius ? 1 : 0];
+    if (!slot.valid) return fail(KNN_ERR_INVALID_ARGUMENT, "no tuned plan for k %u yet", k);
+    std::memset(out, 0, sizeof(*out));
+    out->block_size = slot.plan.block;
+    out->heap_tracking = slot.plan.heap;
+    out->shmem_tracking = slot.plan.sh_nn;
+    out->shmem_stack = slot.plan.sh_stack;
+    out->leaf_scan = slot.plan.leaf_scan;
+    out->reserved[0] = slot.candidates;
+    if (ms) *ms = slot.ms;
+    return KNN_OK;
+}
+
 uint64_t knn_launch_count(void) { return knn::g_launches.load(); }
+
+int knn_radius_model_train(knn_index* index, const float* d_samples, uint32_t count, uint32_t k,
+                           const knn_train_opts* opts, void* stream, knn_train_report* report) {
+    if (!index || !d_samples) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
+    if (index->n == 0) return fail(KNN_ERR_INVALID_ARGUMENT, "empty point set");
+    if (count < 16) return fail(KNN_ERR_INVALID_ARGUMENT, "need at least 16 samples (got %u)", count);
+    if (k == 0 || k > knn::kMaxK) return fail(k ? KNN_ERR_UNSUPPORTED : KNN_ERR_INVALID_ARGUMENT, "k %u", k);
+    knn_train_opts o{};
+    if (opts) o = *opts;
+    if (!o.steps) o.steps = 1500;
+    if (!o.batch) o.batch = 1024;
+    if (!(o.lr > 0.0f)) o.lr = 3e-3f;
+    if (!(o.coverage > 0.0f && o.coverage < 1.0f)) o.coverage = 0.98f;
+    if (!o.seed) o.seed = 1;
+    return knn::model_train(index, d_samples, count, k, o, as_stream(stream), report);
+}
+
+int knn_radius_model_predict(knn_index* index, const float* d_queries, uint32_t count, float* d_log_kth,
+                             void* stream) {
+    if (!index || !d_log_kth || (count && !d_queries)) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
+    if (!index->has_model) return fail(KNN_ERR_NOT_TRAINED, "no radius model attached to this index");
+    if (!count) return KNN_OK;
+    return knn::model_predict(index->model.as<float>(), index->dims, d_queries, count, INFINITY, nullptr, nullptr,
+                              d_log_kth, as_stream(stream));
+}
+
+uint32_t knn_radius_model_size(uint32_t dims) {
+    return dims && dims <= knn::kMaxDims ? static_cast<uint32_t>(knn::model_floats(dims)) : 0u;
+}
+
+int knn_radius_model_export(const knn_index* index, float* h_params, uint32_t capacity) {
+    if (!index || !h_params) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
+    if (!index->has_model) return fail(KNN_ERR_NOT_TRAINED, "no radius model attached to this index");
+    const size_t n = knn::model_floats(index->dims);
+    if (capacity < n) return fail(KNN_ERR_INVALID_ARGUMENT, "capacity %u < %zu", capacity, n);
+    KNN_TRY_CUDA(cudaMemcpy(h_params, index->model.ptr, n * 4, cudaMemcpyDeviceToHost));
+    return KNN_OK;
+}
+
+int knn_radius_model_import(knn_index* index, const float* h_params, uint32_t count, uint32_t k) {
+    if (!index || !h_params) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
+    const size_t n = knn::model_floats(index->dims);
+    if (count != n) return fail(KNN_ERR_INVALID_ARGUMENT, "model for dims %u has %zu floats, got %u", index->dims, n, count);
+    KNN_TRY(index->model.alloc(n * 4));
+    KNN_TRY_CUDA(cudaMemcpy(index->model.ptr, h_params, n * 4, cudaMemcpyHostToDevice));
+    index->has_model = true;
+    index->model_k = k;
+    return KNN_OK;
+}
+
+int knn_radius_model_gradients(const float* h_params, uint32_t dims, const float* h_x, const float* h_targets,
+                               uint32_t batch, float* h_grad, float* h_loss) {
+    if (!h_params || !h_x || !h_targets || !h_grad || !h_loss || !batch)
+        return fail(KNN_ERR_INVALID_ARGUMENT, "null argument or empty batch");
+    if (!dims || dims > knn::kMaxDims) return fail(KNN_ERR_UNSUPPORTED, "dims %u", dims);
+    const size_t np = knn::model_floats(dims);
+    knn::DevBuf buf, scratch;
+    KNN_TRY(buf.alloc(knn::carve_bytes({np * 4, np * 4, static_cast<size_t>(batch) * dims * 4,
+                                        static_cast<size_t>(batch) * 4, static_cast<size_t>(batch) * 4})));
+    knn::Carver c(buf.ptr);
+    float* prm = c.take<float>(np);
+    float* grad = c.take<float>(np);
+    float* x = c.take<float>(static_cast<size_t>(batch) * dims);
+    float* t = c.take<float>(batch);
+    float* loss = c.take<float>(batch);
+    KNN_TRY_CUDA(cudaMemcpy(prm, h_params, np * 4, cudaMemcpyHostToDevice));
+    KNN_TRY_CUDA(cudaMemcpy(x, h_x, static_cast<size_t>(batch) * dims * 4, cudaMemcpyHostToDevice));
+    KNN_TRY_CUDA(cudaMemcpy(t, h_targets, static_cast<size_t>(batch) * 4, cudaMemcpyHostToDevice));
+    KNN_TRY(knn::model_gradients(prm, dims, x, t, nullptr, batch, grad, loss, scratch, nullptr));
+    const size_t trainable = np - 2 * dims - 1;
+    KNN_TRY_CUDA(cudaMemcpy(h_grad, grad, trainable * 4, cudaMemcpyDeviceToHost));
+    std::vector<float> lr(batch);
+    KNN_TRY_CUDA(cudaMemcpy(lr.data(), loss, static_cast<size_t>(batch) * 4, cudaMemcpyDeviceToHost));
+    double total = 0;
+    for (float v : lr) total += v;
+    *h_loss = static_cast<float>(total);
+    return KNN_OK;
+}
 
 const char* knn_status_string(int status) {
     switch (status) {

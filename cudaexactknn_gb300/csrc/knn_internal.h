@@ -191,7 +191,16 @@ struct knn_index {
     // Learned radius model (weights on the device), see radius_model.cu.
     knn::DevBuf model;
     bool has_model = false;
-    float model_scale = 1.0f;
+    uint32_t model_k = 0;     // k the model was trained for
+    knn::DevBuf seed_ws;      // seeded radii, fallback list and count
+
+    // Autotuned plans, one per k class (8, 16, 32, 64, 128) and learned-radius on/off.
+    struct Tuned {
+        bool valid = false;
+        knn::QueryPlan plan;
+        float ms = 0.0f;
+        uint32_t candidates = 0;
+    } tuned[5][2];
 };
 
 namespace knn {
@@ -222,7 +231,21 @@ struct QueryArgs {
     int32_t* out_idx;
     float* out_dist;
     DevCounters* counters;    // null unless instrumented
+    const uint32_t* order = nullptr;      // explicit thread -> query list (no reordering)
+    const uint32_t* count_dev = nullptr;  // device-side count bounding `order` (count is then an upper bound)
 };
+
+// Learned radius model (radius_model.cu).
+size_t model_floats(uint32_t dims);
+int model_gradients(const float* d_prm, uint32_t dims, const float* d_x, const float* d_t, const uint32_t* d_rows,
+                    uint32_t batch, float* d_grad, float* d_loss_rows, DevBuf& scratch, cudaStream_t s);
+int model_predict(const float* d_prm, uint32_t dims, const float* d_x, uint32_t count, float max_d2,
+                  const float* user_radii, float* d_radii, float* d_raw, cudaStream_t s);
+int model_fallbacks(const int32_t* out_idx, uint32_t count, uint32_t k, const float* seeded, float max_d2,
+                    const float* user_radii, uint32_t* list, uint32_t* list_count, DevCounters* counters,
+                    cudaStream_t s);
+int model_train(knn_index* ix, const float* d_samples, uint32_t count, uint32_t k, const knn_train_opts& o,
+                cudaStream_t s, knn_train_report* rep);
 
 int bf_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 int kd_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);

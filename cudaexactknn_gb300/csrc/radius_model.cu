@@ -1,0 +1,372 @@
+// Learned search radius: a D -> 64 -> 64 -> 1 multilayer perceptron that predicts, from a
+// query's coordinates, the logarithm of its k-th neighbour's squared distance.  The prediction
+// plus a calibrated margin seeds each query's search radius (max_distance2); a query that finds
+// fewer than k points inside its seeded radius is searched again without the seed, so answers
+// stay exact and the plain search is both the fallback and the judge.
+//
+// Training runs on the GPU with the kernels below (forward + backward per sample, weight
+// gradients as batch reductions in a fixed order, Adam), on targets produced by the engine's own
+// exact search for sample queries.  The reference has no counterpart: its pruning radius is the
+// caller's single Query::maxDistance2 (src/KnnTrees.cuh:228, used at src/KdTreeGpu.cuh:211 and
+// src/BallTreeGpu.cuh:48).
+//
+// Parameter layout (floats): W1[64][D] b1[64] W2[64][64] b2[64] w3[64] b3, then the input
+// normalisation mu[D] inv_sd[D] and the calibrated margin.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "knn_internal.h"
+
+namespace knn {
+
+constexpr uint32_t kHidden = 64;
+
+struct ModelLayout {
+    uint32_t dims;
+    uint32_t w1, b1, w2, b2, w3, b3, mu, inv_sd, margin, total, trainable;
+    __host__ __device__ explicit ModelLayout(uint32_t d) : dims(d) {
+        w1 = 0;
+        b1 = w1 + kHidden * d;
+        w2 = b1 + kHidden;
+        b2 = w2 + kHidden * kHidden;
+        w3 = b2 + kHidden;
+        b3 = w3 + kHidden;
+        trainable = b3 + 1;
+        mu = trainable;
+        inv_sd = mu + d;
+        margin = inv_sd + d;
+        total = margin + 1;
+    }
+};
+
+namespace {
+
+// Forward (and, with targets, backward) of one sample per thread.  Stores the activations and
+// the back-propagated deltas for the gradient reductions.
+__global__ void mlp_fwd_bwd_kernel(const float* __restrict__ prm, uint32_t dims, const float* __restrict__ x,
+                                   const float* __restrict__ target, const uint32_t* __restrict__ rows,
+                                   uint32_t batch, float* __restrict__ xn_out, float* __restrict__ h1_out,
+                                   float* __restrict__ h2_out, float* __restrict__ d1_out,
+                                   float* __restrict__ d2_out, float* __restrict__ dy_out,
+                                   float* __restrict__ loss_out) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= batch) return;
+    const ModelLayout L(dims);
+    const uint32_t r = rows ? rows[b] : b;
+    float xn[kMaxDims];
+    for (uint32_t d = 0; d < dims; ++d) {
+        xn[d] = (x[static_cast<size_t>(r) * dims + d] - prm[L.mu + d]) * prm[L.inv_sd + d];
+        xn_out[static_cast<size_t>(b) * dims + d] = xn[d];
+    }
+    float h1[kHidden], h2[kHidden];
+    for (uint32_t i = 0; i < kHidden; ++i) {
+        float a = prm[L.b1 + i];
+        for (uint32_t d = 0; d < dims; ++d) a = fmaf(prm[L.w1 + i * dims + d], xn[d], a);
+        h1[i] = fmaxf(a, 0.0f);
+        h1_out[static_cast<size_t>(b) * kHidden + i] = h1[i];
+    }
+    float y = prm[L.b3];
+    for (uint32_t i = 0; i < kHidden; ++i) {
+        float a = prm[L.b2 + i];
+        for (uint32_t j = 0; j < kHidden; ++j) a = fmaf(prm[L.w2 + i * kHidden + j], h1[j], a);
+        h2[i] = fmaxf(a, 0.0f);
+        h2_out[static_cast<size_t>(b) * kHidden + i] = h2[i];
+        y = fmaf(prm[L.w3 + i], h2[i], y);
+    }
+    // Mean squared error on the log distance: loss = mean (y - t)^2.
+    const float err = y - target[r];
+    const float dy = 2.0f * err / static_cast<float>(batch);
+    dy_out[b] = dy;
+    loss_out[b] = err * err / static_cast<float>(batch);
+    float d2[kHidden];
+    for (uint32_t i = 0; i < kHidden; ++i) {
+        d2[i] = h2[i] > 0.0f ? dy * prm[L.w3 + i] : 0.0f;
+        d2_out[static_cast<size_t>(b) * kHidden + i] = d2[i];
+    }
+    for (uint32_t j = 0; j < kHidden; ++j) {
+        float a = 0.0f;
+        for (uint32_t i = 0; i < kHidden; ++i) a = fmaf(prm[L.w2 + i * kHidden + j], d2[i], a);
+        d1_out[static_cast<size_t>(b) * kHidden + j] = h1[j] > 0.0f ? a : 0.0f;
+    }
+}
+
+// One thread per trainable parameter: its gradient summed over the batch in sample order.
+__global__ void mlp_grad_kernel(uint32_t dims, uint32_t batch, const float* __restrict__ xn,
+                                const float* __restrict__ h1, const float* __restrict__ h2,
+                                const float* __restrict__ d1, const float* __restrict__ d2,
+                                const float* __restrict__ dy, float* __restrict__ grad) {
+    const ModelLayout L(dims);
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= L.trainable) return;
+    float g = 0.0f;
+    if (p < L.b1) {
+        const uint32_t i = p / dims, d = p % dims;
+        for (uint32_t b = 0; b < batch; ++b) g = fmaf(d1[b * kHidden + i], xn[b * dims + d], g);
+    } else if (p < L.w2) {
+        const uint32_t i = p - L.b1;
+        for (uint32_t b = 0; b < batch; ++b) g += d1[b * kHidden + i];
+    } else if (p < L.b2) {
+        const uint32_t i = (p - L.w2) / kHidden, j = (p - L.w2) % kHidden;
+        for (uint32_t b = 0; b < batch; ++b) g = fmaf(d2[b * kHidden + i], h1[b * kHidden + j], g);
+    } else if (p < L.w3) {
+        const uint32_t i = p - L.b2;
+        for (uint32_t b = 0; b < batch; ++b) g += d2[b * kHidden + i];
+    } else if (p < L.b3) {
+        const uint32_t j = p - L.w3;
+        for (uint32_t b = 0; b < batch; ++b) g = fmaf(dy[b], h2[b * kHidden + j], g);
+    } else {
+        for (uint32_t b = 0; b < batch; ++b) g += dy[b];
+    }
+    grad[p] = g;
+}
+
+// Adam (Kingma & Ba, 2015) with bias correction.
+__global__ void adam_kernel(float* __restrict__ prm, const float* __restrict__ grad, float* __restrict__ m,
+                            float* __restrict__ v, uint32_t n, float lr, float beta1, float beta2, float eps,
+                            float corr1, float corr2) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float g = grad[p];
+    const float mp = beta1 * m[p] + (1.0f - beta1) * g;
+    const float vp = beta2 * v[p] + (1.0f - beta2) * g * g;
+    m[p] = mp;
+    v[p] = vp;
+    prm[p] -= lr * (mp / corr1) / (sqrtf(vp / corr2) + eps);
+}
+
+// Seeded radius of each query: min(exp(prediction + margin), the caller's radius).
+__global__ void mlp_infer_kernel(const float* __restrict__ prm, uint32_t dims, const float* __restrict__ x,
+                                 uint32_t count, float max_d2, const float* __restrict__ user_radii,
+                                 float* __restrict__ radii, float* __restrict__ raw) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count) return;
+    const ModelLayout L(dims);
+    float xn[kMaxDims];
+    for (uint32_t d = 0; d < dims; ++d)
+        xn[d] = (x[static_cast<size_t>(q) * dims + d] - __ldg(prm + L.mu + d)) * __ldg(prm + L.inv_sd + d);
+    float h1[kHidden];
+    for (uint32_t i = 0; i < kHidden; ++i) {
+        float a = __ldg(prm + L.b1 + i);
+        for (uint32_t d = 0; d < dims; ++d) a = fmaf(__ldg(prm + L.w1 + i * dims + d), xn[d], a);
+        h1[i] = fmaxf(a, 0.0f);
+    }
+    float y = __ldg(prm + L.b3);
+    for (uint32_t i = 0; i < kHidden; ++i) {
+        float a = __ldg(prm + L.b2 + i);
+#pragma unroll 16
+        for (uint32_t j = 0; j < kHidden; ++j) a = fmaf(__ldg(prm + L.w2 + i * kHidden + j), h1[j], a);
+        y = fmaf(__ldg(prm + L.w3 + i), fmaxf(a, 0.0f), y);
+    }
+    if (raw) raw[q] = y;
+    if (radii) {
+        const float cap = user_radii ? user_radii[q] : max_d2;
+        const float r = __expf(fminf(y + __ldg(prm + L.margin), 80.0f));
+        radii[q] = fminf(r, cap);
+    }
+}
+
+// Queries whose seeded radius was below the caller's and that found fewer than k points.
+__global__ void fallback_kernel(const int32_t* __restrict__ out_idx, uint32_t count, uint32_t k,
+                                const float* __restrict__ seeded, float max_d2, const float* __restrict__ user_radii,
+                                uint32_t* __restrict__ list, uint32_t* __restrict__ list_count,
+                                DevCounters* counters) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count) return;
+    const float cap = user_radii ? user_radii[q] : max_d2;
+    if (seeded[q] < cap && out_idx[static_cast<size_t>(q) * k + (k - 1)] < 0) {
+        list[atomicAdd(list_count, 1u)] = q;
+        if (counters) atomicAdd(&counters->fallback, 1ull);
+    }
+}
+
+__global__ void kth_log_kernel(const float* __restrict__ dist, const int32_t* __restrict__ idx, uint32_t count,
+                               uint32_t k, float* __restrict__ target) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count) return;
+    const float d = dist[static_cast<size_t>(q) * k + (k - 1)];
+    target[q] = logf(fmaxf(d, 1e-30f));
+    (void)idx;
+}
+
+}  // namespace
+
+size_t model_floats(uint32_t dims) { return ModelLayout(dims).total; }
+
+// Forward + backward for `batch` samples with the given parameters; writes gradients and the
+// summed loss (used by training and by the gradient check).
+int model_gradients(const float* d_prm, uint32_t dims, const float* d_x, const float* d_t, const uint32_t* d_rows,
+                    uint32_t batch, float* d_grad, float* d_loss_rows, DevBuf& scratch, cudaStream_t s) {
+    const size_t need = carve_bytes({static_cast<size_t>(batch) * dims * 4, static_cast<size_t>(batch) * kHidden * 4,
+                                     static_cast<size_t>(batch) * kHidden * 4, static_cast<size_t>(batch) * kHidden * 4,
+                                     static_cast<size_t>(batch) * kHidden * 4, static_cast<size_t>(batch) * 4});
+    KNN_TRY(scratch.reserve(need));
+    Carver c(scratch.ptr);
+    float* xn = c.take<float>(static_cast<size_t>(batch) * dims);
+    float* h1 = c.take<float>(static_cast<size_t>(batch) * kHidden);
+    float* h2 = c.take<float>(static_cast<size_t>(batch) * kHidden);
+    float* d1 = c.take<float>(static_cast<size_t>(batch) * kHidden);
+    float* d2 = c.take<float>(static_cast<size_t>(batch) * kHidden);
+    float* dy = c.take<float>(batch);
+    mlp_fwd_bwd_kernel<<<ceil_div(batch, 128), 128, 0, s>>>(d_prm, dims, d_x, d_t, d_rows, batch, xn, h1, h2, d1,
+                                                            d2, dy, d_loss_rows);
+    const ModelLayout L(dims);
+    mlp_grad_kernel<<<ceil_div(L.trainable, 128), 128, 0, s>>>(dims, batch, xn, h1, h2, d1, d2, dy, d_grad);
+    KNN_LAUNCHED_N(2);
+    return KNN_OK;
+}
+
+int model_predict(const float* d_prm, uint32_t dims, const float* d_x, uint32_t count, float max_d2,
+                  const float* user_radii, float* d_radii, float* d_raw, cudaStream_t s) {
+    mlp_infer_kernel<<<ceil_div(count, 128), 128, 0, s>>>(d_prm, dims, d_x, count, max_d2, user_radii, d_radii,
+                                                          d_raw);
+    KNN_LAUNCHED();
+    return KNN_OK;
+}
+
+int model_fallbacks(const int32_t* out_idx, uint32_t count, uint32_t k, const float* seeded, float max_d2,
+                    const float* user_radii, uint32_t* list, uint32_t* list_count, DevCounters* counters,
+                    cudaStream_t s) {
+    KNN_TRY_CUDA(cudaMemsetAsync(list_count, 0, sizeof(uint32_t), s));
+    fallback_kernel<<<ceil_div(count, 256), 256, 0, s>>>(out_idx, count, k, seeded, max_d2, user_radii, list,
+                                                         list_count, counters);
+    KNN_LAUNCHED();
+    return KNN_OK;
+}
+
+int model_train(knn_index* ix, const float* d_samples, uint32_t count, uint32_t k, const knn_train_opts& o,
+                cudaStream_t s, knn_train_report* rep) {
+    const uint32_t dims = ix->dims;
+    const ModelLayout L(dims);
+    cudaEvent_t e0, e1;
+    KNN_TRY_CUDA(cudaEventCreate(&e0));
+    KNN_TRY_CUDA(cudaEventCreate(&e1));
+    KNN_TRY_CUDA(cudaEventRecord(e0, s));
+
+    // 1. Exact k-th distances of the samples, from the engine's own plain search.
+    DevBuf buf;
+    const size_t ck = static_cast<size_t>(count) * k;
+    const size_t pb = static_cast<size_t>(L.total) * 4;
+    KNN_TRY(buf.alloc(carve_bytes({ck * 4, ck * 4, static_cast<size_t>(count) * 4, static_cast<size_t>(count) * 4,
+                                   pb, pb, pb, pb, static_cast<size_t>(o.batch) * 4})));
+    Carver c(buf.ptr);
+    int32_t* idx = c.take<int32_t>(ck);
+    float* dist = c.take<float>(ck);
+    float* target = c.take<float>(count);
+    uint32_t* rows = c.take<uint32_t>(count);
+    float* prm = c.take<float>(L.total);
+    float* grad = c.take<float>(L.total);
+    float* m = c.take<float>(L.total);
+    float* v = c.take<float>(L.total);
+    float* loss_rows = c.take<float>(o.batch);
+    QueryArgs qa{d_samples, count, INFINITY, nullptr, k, idx, dist, nullptr};
+    QueryPlan plan;
+    switch (ix->structure) {
+        case KNN_BRUTE_FORCE: KNN_TRY(bf_query(ix, qa, plan, s)); break;
+        case KNN_KD_TREE: KNN_TRY(kd_query(ix, qa, plan, s)); break;
+        default: KNN_TRY(ball_query(ix, qa, plan, s)); break;
+    }
+    kth_log_kernel<<<ceil_div(count, 256), 256, 0, s>>>(dist, idx, count, k, target);
+    KNN_LAUNCHED();
+
+    // 2. Input normalisation and initial weights (seeded, He-style scaling), on the host.
+    std::vector<float> hx(static_cast<size_t>(count) * dims), ht(count);
+    KNN_TRY_CUDA(cudaMemcpyAsync(hx.data(), d_samples, hx.size() * 4, cudaMemcpyDeviceToHost, s));
+    KNN_TRY_CUDA(cudaMemcpyAsync(ht.data(), target, ht.size() * 4, cudaMemcpyDeviceToHost, s));
+    KNN_TRY_CUDA(cudaStreamSynchronize(s));
+    std::vector<float> hp(L.total, 0.0f);
+    for (uint32_t d = 0; d < dims; ++d) {
+        double mean = 0, sq = 0;
+        for (uint32_t i = 0; i < count; ++i) mean += hx[static_cast<size_t>(i) * dims + d];
+        mean /= count;
+        for (uint32_t i = 0; i < count; ++i) {
+            const double t = hx[static_cast<size_t>(i) * dims + d] - mean;
+            sq += t * t;
+        }
+        const double sd = std::sqrt(sq / std::max(1u, count)) + 1e-12;
+        hp[L.mu + d] = static_cast<float>(mean);
+        hp[L.inv_sd + d] = static_cast<float>(1.0 / sd);
+    }
+    double tmean = 0;
+    for (float t : ht) tmean += t;
+    tmean /= std::max(1u, count);
+    std::mt19937 gen(o.seed);
+    std::normal_distribution<float> nd(0.0f, 1.0f);
+    for (uint32_t i = 0; i < kHidden * dims; ++i) hp[L.w1 + i] = nd(gen) * std::sqrt(2.0f / dims);
+    for (uint32_t i = 0; i < kHidden * kHidden; ++i) hp[L.w2 + i] = nd(gen) * std::sqrt(2.0f / kHidden);
+    for (uint32_t i = 0; i < kHidden; ++i) hp[L.w3 + i] = nd(gen) * std::sqrt(1.0f / kHidden);
+    hp[L.b3] = static_cast<float>(tmean);
+    KNN_TRY_CUDA(cudaMemcpyAsync(prm, hp.data(), hp.size() * 4, cudaMemcpyHostToDevice, s));
+    KNN_TRY_CUDA(cudaMemsetAsync(m, 0, L.total * 4, s));
+    KNN_TRY_CUDA(cudaMemsetAsync(v, 0, L.total * 4, s));
+
+    // 3. Adam over shuffled minibatches.
+    std::vector<uint32_t> perm(count);
+    for (uint32_t i = 0; i < count; ++i) perm[i] = i;
+    std::shuffle(perm.begin(), perm.end(), gen);
+    KNN_TRY_CUDA(cudaMemcpyAsync(rows, perm.data(), count * 4, cudaMemcpyHostToDevice, s));
+    DevBuf scratch;
+    const uint32_t batch = std::min(o.batch, count);
+    const float b1 = 0.9f, b2 = 0.999f;
+    float c1 = 1.0f, c2 = 1.0f;
+    uint32_t offset = 0;
+    for (uint32_t step = 0; step < o.steps; ++step) {
+        if (offset + batch > count) offset = 0;
+        KNN_TRY(model_gradients(prm, dims, d_samples, target, rows + offset, batch, grad, loss_rows, scratch, s));
+        c1 *= b1;
+        c2 *= b2;
+        const float lr = o.lr * (step < o.steps / 2 ? 1.0f : (step < 3 * o.steps / 4 ? 0.3f : 0.1f));
+        adam_kernel<<<ceil_div(L.trainable, 256), 256, 0, s>>>(prm, grad, m, v, L.trainable, lr, b1, b2, 1e-8f,
+                                                              1.0f - c1, 1.0f - c2);
+        KNN_LAUNCHED();
+        offset += batch;
+    }
+    std::vector<float> hl(batch);
+    KNN_TRY_CUDA(cudaMemcpyAsync(hl.data(), loss_rows, batch * 4, cudaMemcpyDeviceToHost, s));
+
+    // 4. Margin: the `coverage` quantile of (target - prediction) over the samples.
+    KNN_TRY(model_predict(prm, dims, d_samples, count, INFINITY, nullptr, nullptr, dist, s));
+    std::vector<float> pred(count);
+    KNN_TRY_CUDA(cudaMemcpyAsync(pred.data(), dist, count * 4, cudaMemcpyDeviceToHost, s));
+    KNN_TRY_CUDA(cudaStreamSynchronize(s));
+    std::vector<float> resid(count);
+    double sse = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        resid[i] = ht[i] - pred[i];
+        sse += static_cast<double>(resid[i]) * resid[i];
+    }
+    std::vector<float> sorted = resid;
+    const uint32_t qi = std::min<uint32_t>(count - 1, static_cast<uint32_t>(std::ceil(o.coverage * count)));
+    std::nth_element(sorted.begin(), sorted.begin() + qi, sorted.end());
+    const float margin = sorted[qi] + 1e-3f;
+    KNN_TRY_CUDA(cudaMemcpyAsync(prm + L.margin, &margin, 4, cudaMemcpyHostToDevice, s));
+
+    KNN_TRY(ix->model.alloc(L.total * 4));
+    KNN_TRY_CUDA(cudaMemcpyAsync(ix->model.ptr, prm, L.total * 4, cudaMemcpyDeviceToDevice, s));
+    KNN_TRY_CUDA(cudaEventRecord(e1, s));
+    KNN_TRY_CUDA(cudaEventSynchronize(e1));
+    ix->has_model = true;
+    ix->model_k = k;
+    if (rep) {
+        std::memset(rep, 0, sizeof(*rep));
+        KNN_TRY_CUDA(cudaEventElapsedTime(&rep->train_ms, e0, e1));
+        double bl = 0;
+        for (float l : hl) bl += l;
+        rep->final_batch_loss = static_cast<float>(bl);
+        rep->rmse = static_cast<float>(std::sqrt(sse / count));
+        rep->margin = margin;
+        uint32_t covered = 0;
+        for (float r : resid) covered += r <= margin ? 1u : 0u;
+        rep->coverage = static_cast<float>(covered) / count;
+        rep->samples = count;
+        rep->steps = o.steps;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return KNN_OK;
+}
+
+}  // namespace knn

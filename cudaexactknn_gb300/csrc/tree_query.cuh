@@ -30,6 +30,27 @@ __device__ __forceinline__ float slot_dist(const float (&q)[DP], const float* __
     }
 }
 
+// Slots under node `node` at depth `depth` of a tree whose leaves sit at depth `leaf_depth`:
+// the subtree's leaves are contiguous, so its slots are one range.
+struct SlotRange {
+    size_t first;
+    uint32_t count;
+};
+__device__ __forceinline__ SlotRange subtree_slots(uint32_t node, uint32_t depth, uint32_t leaf_depth,
+                                                  uint32_t node_count, uint32_t leaf_slots) {
+    const uint32_t span = leaf_depth - depth;
+    const uint64_t first_leaf = ((static_cast<uint64_t>(node) + 1) << span) - 1 - node_count;
+    return SlotRange{static_cast<size_t>(first_leaf) * leaf_slots, leaf_slots << span};
+}
+
+// Scan depth for a plan: stop `levels` above the leaves so that a scanned range holds at most
+// `max_points` slots (0 keeps the tree's own leaves).
+inline uint32_t scan_depth_for(uint32_t node_depth, uint32_t leaf_slots, uint32_t max_points) {
+    uint32_t levels = 0;
+    while (levels < node_depth && (static_cast<uint64_t>(leaf_slots) << (levels + 1)) <= max_points) ++levels;
+    return node_depth - levels;
+}
+
 // Index of the point in a leaf slot, without its coordinates.
 template <int DP>
 __device__ __forceinline__ int32_t slot_id(const float* __restrict__ slot) {

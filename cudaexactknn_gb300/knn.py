@@ -159,6 +159,38 @@ class _Index:
         _lib.check(st)
         return out_idx, out_dist
 
+    # ---- learned radius ---------------------------------------------------------------------
+    def train_radius_model(self, samples: torch.Tensor, k: int, steps: int = 0, batch: int = 0, lr: float = 0.0,
+                           coverage: float = 0.0, seed: int = 0, stream=None) -> _lib.TrainReport:
+        """Trains the index's radius model on sample queries (CUDA float32 [count, dims])."""
+        s = _check_points(samples, "samples")
+        o = _lib.TrainOpts()
+        o.steps, o.batch, o.lr, o.coverage, o.seed = steps, batch, lr, coverage, seed
+        rep = _lib.TrainReport()
+        _lib.check(_lib.load().knn_radius_model_train(self._h, s.data_ptr(), int(s.shape[0]), k, ctypes.byref(o),
+                                                      _stream_handle(stream), ctypes.byref(rep)))
+        return rep
+
+    def predict_log_kth(self, queries: torch.Tensor) -> torch.Tensor:
+        q = _check_points(queries, "queries")
+        out = torch.empty(q.shape[0], dtype=torch.float32, device=q.device)
+        _lib.check(_lib.load().knn_radius_model_predict(self._h, q.data_ptr(), int(q.shape[0]), out.data_ptr(),
+                                                        _stream_handle(None)))
+        return out
+
+    def export_radius_model(self):
+        import numpy as np
+        lib = _lib.load()
+        n = lib.knn_radius_model_size(self.dims)
+        out = np.empty(n, dtype=np.float32)
+        _lib.check(lib.knn_radius_model_export(self._h, out.ctypes.data, n))
+        return out
+
+    def import_radius_model(self, params, k: int) -> None:
+        import numpy as np
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        _lib.check(_lib.load().knn_radius_model_import(self._h, p.ctypes.data, p.size, k))
+
     def stats(self, query: Query, k: int, **kw) -> _lib.QueryCounters:
         """Runs the query with device counters (nodes visited, leaves, points scanned)."""
         q = _check_points(query.points)
@@ -225,3 +257,19 @@ def build_index(structure: str, points: torch.Tensor, depth_skips: int | None = 
     if structure == "ball":
         return BallTreeGpu(points, depth_skips=1 if depth_skips is None else depth_skips, **kw)
     raise ValueError(structure)
+
+
+def radius_model_gradients(params, dims: int, x, targets):
+    """Forward + backward of the radius model on the GPU for a host batch: (loss, gradients)."""
+    import numpy as np
+    lib = _lib.load()
+    p = np.ascontiguousarray(params, np.float32)
+    xb = np.ascontiguousarray(x, np.float32)
+    tb = np.ascontiguousarray(targets, np.float32)
+    n = lib.knn_radius_model_size(dims)
+    trainable = n - 2 * dims - 1
+    grad = np.empty(trainable, np.float32)
+    loss = ctypes.c_float()
+    _lib.check(lib.knn_radius_model_gradients(p.ctypes.data, dims, xb.ctypes.data, tb.ctypes.data, len(tb),
+                                              grad.ctypes.data, ctypes.byref(loss)))
+    return loss.value, grad

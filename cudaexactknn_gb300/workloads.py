@@ -105,11 +105,14 @@ def c1(scale: float = 1.0) -> Workload:
 
 
 def c2(scale: float = 1.0) -> Workload:
+    # extra["train"]: sample queries for the learned radius, 65,536 further draws of the same
+    # mixture (seeded apart from the benchmark queries); likewise for c3 and c4.
     rng = _rng(1002)
     n, q = int(4194304 * scale), int(1048576 * scale)
     pts, centres = mixture(rng, n, 3, 64, 0.01)
     qs, _ = mixture(rng, q, 3, 64, 0.01, centres)
-    return Workload("c2_kd3_n4194304_q1048576_k16", "kd", pts, qs, 16, INF, 0)
+    train, _ = mixture(_rng(2002), 65536, 3, 64, 0.01, centres)
+    return Workload("c2_kd3_n4194304_q1048576_k16", "kd", pts, qs, 16, INF, 0, extra={"train": train})
 
 
 def c3(scale: float = 1.0) -> Workload:
@@ -117,7 +120,8 @@ def c3(scale: float = 1.0) -> Workload:
     n, q = int(1048576 * scale), int(262144 * scale)
     pts, basis = subspace(rng, n, 16, 4, 0.05)
     qs, _ = subspace(rng, q, 16, 4, 0.05, basis)
-    return Workload("c3_ball16_n1048576_q262144_k32", "ball", pts, qs, 32, INF, 1)
+    train, _ = subspace(_rng(2003), 65536, 16, 4, 0.05, basis)
+    return Workload("c3_ball16_n1048576_q262144_k32", "ball", pts, qs, 32, INF, 1, extra={"train": train})
 
 
 def c4(scale: float = 1.0) -> Workload:
@@ -125,7 +129,8 @@ def c4(scale: float = 1.0) -> Workload:
     n, q = int(1048576 * scale), int(65536 * scale)
     pts, centres = gauss_mix(rng, n, 128, 256, 0.3)
     qs, _ = gauss_mix(rng, q, 128, 256, 0.3, centres)
-    return Workload("c4_bf128_n1048576_q65536_k100", "bf", pts, qs, 100, INF, 0)
+    train, _ = gauss_mix(_rng(2004), 16384, 128, 256, 0.3, centres)
+    return Workload("c4_bf128_n1048576_q65536_k100", "bf", pts, qs, 100, INF, 0, extra={"train": train})
 
 
 def c5_sets(scale: float = 1.0, count: int = 64) -> list[Workload]:

@@ -4,6 +4,14 @@
 // (src/BallTreeGpu.cuh:463-650).
 #pragma once
 
+// Standard headers the reference's version brings in (directly or through <cub/cub.cuh>);
+// code written against the reference may rely on them.
+#include <algorithm>
+#include <cassert>
+#include <cstring>
+#include <limits>
+#include <numeric>
+
 #include "KnnTrees.cuh"
 
 namespace KnnTrees {

@@ -3,6 +3,14 @@
 // depthSkips, and batchKnn<K, BLOCK_SIZE, HEAP, SH_NN, SH_STACK> (src/KdTreeGpu.cuh:444-574).
 #pragma once
 
+// Standard headers the reference's version brings in (directly or through <cub/cub.cuh>);
+// code written against the reference may rely on them.
+#include <algorithm>
+#include <cassert>
+#include <cstring>
+#include <limits>
+#include <numeric>
+
 #include "KnnTrees.cuh"
 
 namespace KnnTrees {

@@ -25,7 +25,7 @@
 #include <string>
 #include <sys/types.h>
 
-#include "../cudaexactknn.h"
+#include "cudaexactknn.h"  // needs -I<repo>/include
 
 namespace KnnTrees {
 

@@ -121,6 +121,28 @@ typedef struct knn_index_info {
     uint32_t radius_model;/* 1 when a learned radius model is attached */
 } knn_index_info;
 
+/* Learned-radius training options; zeros select the defaults in brackets. */
+typedef struct knn_train_opts {
+    uint32_t steps;   /* Adam steps [1500] */
+    uint32_t batch;   /* samples per step [1024] */
+    float lr;         /* learning rate [3e-3] */
+    float coverage;   /* fraction of training queries whose k-th distance must fall inside the
+                         seeded radius; sets the calibrated margin [0.98] */
+    uint32_t seed;    /* weight initialisation and shuffling [1] */
+    uint32_t reserved[3];
+} knn_train_opts;
+
+typedef struct knn_train_report {
+    float train_ms;          /* device time: exact targets + training + calibration */
+    float final_batch_loss;  /* mean squared error on log k-th distance, last minibatch */
+    float rmse;              /* over all samples */
+    float margin;            /* added to the predicted log k-th distance */
+    float coverage;          /* achieved on the samples */
+    uint32_t samples;
+    uint32_t steps;
+    uint32_t reserved;
+} knn_train_report;
+
 /* ---- construction (points: device pointer, float32 [n][dims]; read during the call only) --- */
 KNN_API int knn_bf_create(const float* d_points, uint32_t n, uint32_t dims, void* stream,
                   knn_index** out);
@@ -152,9 +174,34 @@ KNN_API int knn_query_stats(knn_index* index, const float* d_queries, uint32_t c
                     float max_distance2, uint32_t k, int32_t* d_indexes, float* d_distances,
                     const knn_query_opts* opts, void* stream, knn_query_counters* out);
 
+/* ---- learned radius (no counterpart in the reference; it seeds Query::maxDistance2,
+ *      src/KnnTrees.cuh:228, per query) ---------------------------------------------------------
+ * Trains the index's D->64->64->1 radius model on `count` sample queries (device float32
+ * [count][dims]): exact k-th distances from the engine's own search are the targets; forward,
+ * backward and Adam run on the GPU; the margin is calibrated to `coverage`.  Synchronous. */
+KNN_API int knn_radius_model_train(knn_index* index, const float* d_samples, uint32_t count, uint32_t k,
+                                   const knn_train_opts* opts, void* stream, knn_train_report* report);
+/* Predicted natural log of the k-th squared distance per query (device float32 [count]). */
+KNN_API int knn_radius_model_predict(knn_index* index, const float* d_queries, uint32_t count,
+                                     float* d_log_kth, void* stream);
+/* Parameter count of a model for `dims`, and host copies in and out (serialisation). */
+KNN_API uint32_t knn_radius_model_size(uint32_t dims);
+KNN_API int knn_radius_model_export(const knn_index* index, float* h_params, uint32_t capacity);
+KNN_API int knn_radius_model_import(knn_index* index, const float* h_params, uint32_t count, uint32_t k);
+/* Forward + backward of the model on a host batch (x [batch][dims], targets [batch]) with host
+ * parameters; writes the loss and the gradient of every trainable parameter (gradient checks). */
+KNN_API int knn_radius_model_gradients(const float* h_params, uint32_t dims, const float* h_x,
+                                       const float* h_targets, uint32_t batch, float* h_grad, float* h_loss);
+
 /* Device time (ms) of the index's last KNN_QF_TIMING query: the whole query and its main search
  * kernel alone (CUDA events on the query's stream; waits for the query to finish). */
 KNN_API int knn_last_query_timing(knn_index* index, float* total_ms, float* kernel_ms);
+
+/* The plan KNN_QF_AUTOTUNE chose for this index and k (block size, tracking, storage, leaf
+ * bucket), with the tuning sample's time in *ms and the number of candidates timed in
+ * out->reserved[0].  Autotuning runs on the first KNN_QF_AUTOTUNE query per k class. */
+KNN_API int knn_tuned_plan(const knn_index* index, uint32_t k, uint32_t learned_radius, knn_query_opts* out,
+                           float* ms);
 
 /* Number of kernels this library has launched since it was loaded (all indexes, all threads). */
 KNN_API uint64_t knn_launch_count(void);

@@ -1,0 +1,39 @@
+"""The reference's own test program compiles unchanged against the drop-in headers.
+
+tests/FunctionalityTests.cu of the reference includes "../src/BruteForce.cuh" (CPU classes,
+kept as the reference's own code) and "../src/{KnnTrees,BruteForceGpu,KdTreeGpu,BallTreeGpu}.cuh".
+Here a temporary tree puts the drop-in headers at those paths (symbolic links, nothing copied)
+and nvcc builds and links the program against libcudaexactknn.so.  It needs the reference
+sources, so it is skipped where they are not mounted; running the binary needs a GPU, and the
+same assertions run on the GPU through tests/cpp/functionality.cu."""
+
+import os
+import subprocess
+import tempfile
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = "/root/reference"
+DROPIN = os.path.join(ROOT, "include", "KnnTrees")
+LIBDIR = os.path.join(ROOT, "cudaexactknn_gb300")
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "tests")), reason="reference sources not mounted")
+def test_reference_functionality_test_builds_against_dropin():
+    with tempfile.TemporaryDirectory() as tmp:
+        os.makedirs(os.path.join(tmp, "src"))
+        os.makedirs(os.path.join(tmp, "tests"))
+        for name in ("BruteForce.cuh", "KdTree.cuh", "BallTree.cuh"):
+            os.symlink(os.path.join(REF, "src", name), os.path.join(tmp, "src", name))
+        for name in ("KnnTrees.cuh", "BruteForceGpu.cuh", "KdTreeGpu.cuh", "BallTreeGpu.cuh"):
+            os.symlink(os.path.join(DROPIN, name), os.path.join(tmp, "src", name))
+        for name in ("FunctionalityTests.cu", "Tests.cuh"):
+            os.symlink(os.path.join(REF, "tests", name), os.path.join(tmp, "tests", name))
+        out = os.path.join(tmp, "FunctionalityTests")
+        cmd = ["nvcc", "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
+               f"-I{os.path.join(ROOT, 'include')}", os.path.join(tmp, "tests", "FunctionalityTests.cu"),
+               "-o", out, f"-L{LIBDIR}", "-lcudaexactknn", f"-Xlinker=-rpath,{LIBDIR}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-4000:]
+        assert os.path.exists(out)

@@ -231,3 +231,35 @@ def test_build_shape_matches_reference_rules():
         ix = gu.make_index("ball" if ball else "kd", W.uniform(rng, n, 3), skips)
         info = ix.info()
         assert (info.node_depth, info.leaf_slots, info.node_count) == oracle.tree_shape(n, skips, ball)
+
+
+# ---- autotuned plans -------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("structure,dims,k", [("kd", 3, 16), ("ball", 16, 32), ("bf", 8, 10)])
+def test_autotune_is_exact_and_reports_its_plan(structure, dims, k):
+    import ctypes
+    from cudaexactknn_gb300 import _lib
+    rng = np.random.default_rng(dims)
+    pts = W.uniform(rng, 40000, dims)
+    qs = W.uniform(rng, 9000, dims)
+    ix = gu.make_index(structure, pts, 0 if structure == "kd" else 1)
+    want = _oracle(pts, qs, k)
+    gu.assert_rows_equal(*gu.run(ix, qs, k, flags=_lib.QF_AUTOTUNE), *want, what=f"{structure} autotune")
+    o = _lib.QueryOpts()
+    ms = ctypes.c_float()
+    _lib.check(_lib.load().knn_tuned_plan(ix.handle, k, 0, ctypes.byref(o), ctypes.byref(ms)))
+    assert o.block_size in (32, 64, 128, 256) and ms.value > 0
+    assert o.reserved[0] >= (7 if structure == "bf" else 10)
+    # The tuned plan is reused on later calls and still exact.
+    gu.assert_rows_equal(*gu.run(ix, qs, k, flags=_lib.QF_AUTOTUNE), *want, what=f"{structure} autotune again")
+
+
+@pytest.mark.parametrize("leaf_scan", [2, 8, 32, 100000])
+@pytest.mark.parametrize("structure", ["kd", "ball"])
+def test_leaf_bucket_scan(structure, leaf_scan):
+    rng = np.random.default_rng(leaf_scan)
+    pts = W.uniform(rng, 5001, 4)
+    qs = W.uniform(rng, 700, 4)
+    want = _oracle(pts, qs, 9)
+    ix = gu.make_index(structure, pts, 1)
+    gu.assert_rows_equal(*gu.run(ix, qs, 9, leaf_scan=leaf_scan), *want, what=f"{structure} leaf_scan={leaf_scan}")

@@ -1,0 +1,97 @@
+"""Learned search radius: gradients of the GPU kernels against a float64 NumPy oracle, and exact
+answers (with fallbacks) when the model seeds the search."""
+
+import numpy as np
+import pytest
+
+import oracle
+import radius_model_ref as ref
+from cudaexactknn_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+gu = pytest.importorskip("gpu_util")
+
+
+def _random_params(d, rng):
+    n = 64 * d + 64 + 64 * 64 + 64 + 64 + 1
+    p = np.zeros(n + 2 * d + 1, np.float32)
+    p[:n] = rng.standard_normal(n).astype(np.float32) * 0.3
+    p[n:n + d] = rng.standard_normal(d) * 0.1          # mu
+    p[n + d:n + 2 * d] = 1.0 + rng.random(d)            # inv_sd
+    return p
+
+
+@pytest.mark.parametrize("d", [3, 16, 32])
+def test_gradients_match_float64_oracle(d):
+    from cudaexactknn_gb300 import knn
+    rng = np.random.default_rng(d)
+    p = _random_params(d, rng)
+    x = rng.standard_normal((257, d)).astype(np.float32)
+    t = rng.standard_normal(257).astype(np.float32)
+    loss, grad = knn.radius_model_gradients(p, d, x, t)
+    want_loss, want_grad = ref.loss_and_grad(p, d, x, t)
+    assert abs(loss - want_loss) <= 1e-4 * max(1.0, abs(want_loss))
+    scale = np.abs(want_grad).max()
+    np.testing.assert_allclose(grad, want_grad, rtol=2e-3, atol=2e-5 * scale)
+
+
+def test_gradients_match_finite_differences():
+    from cudaexactknn_gb300 import knn
+    rng = np.random.default_rng(5)
+    d = 3
+    p = _random_params(d, rng).astype(np.float64)
+    x = rng.standard_normal((64, d))
+    t = rng.standard_normal(64)
+    _, g = knn.radius_model_gradients(p, d, x, t)
+    for i in rng.choice(len(g), size=25, replace=False):
+        e = np.zeros_like(p)
+        e[i] = 1e-3
+        num = (ref.loss_and_grad(p + e, d, x, t)[0] - ref.loss_and_grad(p - e, d, x, t)[0]) / 2e-3
+        assert abs(g[i] - num) <= 2e-3 * max(1.0, abs(num)), i
+
+
+@pytest.mark.parametrize("structure,skips,d,k", [("kd", 0, 3, 16), ("ball", 1, 16, 32), ("bf", 0, 8, 10)])
+def test_learned_radius_is_exact_and_falls_back(structure, skips, d, k):
+    import torch
+    from cudaexactknn_gb300 import _lib
+    rng = np.random.default_rng(100 + d)
+    if d == 16:
+        pts, basis = W.subspace(rng, 60000, 16, 4, 0.05)
+        qs, _ = W.subspace(rng, 8000, 16, 4, 0.05, basis)
+        train, _ = W.subspace(rng, 8192, 16, 4, 0.05, basis)
+    else:
+        pts, centres = W.mixture(rng, 60000, d, 16, 0.02)
+        qs, _ = W.mixture(rng, 8000, d, 16, 0.02, centres)
+        train, _ = W.mixture(rng, 8192, d, 16, 0.02, centres)
+    ix = gu.make_index(structure, pts, skips)
+    rep = ix.train_radius_model(gu.to_dev(train), k, steps=400)
+    assert rep.samples == 8192 and 0.9 <= rep.coverage <= 1.0
+    # Predictions match the float64 model on the exported parameters.
+    params = ix.export_radius_model()
+    pred = ix.predict_log_kth(gu.to_dev(qs[:500])).cpu().numpy()
+    np.testing.assert_allclose(pred, ref.predict(params, d, qs[:500]), rtol=1e-4, atol=1e-3)
+    want = oracle.bf_knn(pts, qs, k, fma=True, threads=8)
+    got = gu.run(ix, qs, k, flags=_lib.QF_LEARNED_RADIUS)
+    gu.assert_rows_equal(*got, *want, what=f"{structure} learned radius")
+    # Range-limited queries stay exact too (the seed never exceeds the caller's radius).
+    r2 = float(np.quantile(want[1][:, -1], 0.5))
+    got = gu.run(ix, qs, k, r2, flags=_lib.QF_LEARNED_RADIUS)
+    gu.assert_rows_equal(*got, *oracle.bf_knn(pts, qs, k, r2, fma=True, threads=8), what="learned + radius")
+    # A model with its margin forced very negative makes every query fall back: still exact.
+    bad = params.copy()
+    bad[-1] = -20.0
+    ix.import_radius_model(bad, k)
+    from cudaexactknn_gb300 import knn
+    q = knn.Query(gu.to_dev(qs), len(qs), float("inf"))
+    c = ix.stats(q, k, flags=_lib.QF_LEARNED_RADIUS)
+    assert c.fallback_queries == len(qs)
+    gu.assert_rows_equal(q.r_indexes.cpu().numpy(), q.r_distances.cpu().numpy(), *want, what="all fall back")
+
+
+def test_untrained_index_refuses_learned_radius():
+    from cudaexactknn_gb300 import KnnError, _lib
+    rng = np.random.default_rng(0)
+    ix = gu.make_index("kd", W.uniform(rng, 1000, 3))
+    with pytest.raises(KnnError) as e:
+        gu.run(ix, W.uniform(rng, 10, 3), 4, flags=_lib.QF_LEARNED_RADIUS)
+    assert e.value.status == _lib.ERR_NOT_TRAINED
