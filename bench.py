@@ -55,8 +55,9 @@ def parse_args():
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (debug only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-once", action="store_true",
-                    help="build the index, run one chosen-form query and exit (for ncu captures)")
+    ap.add_argument("--profile-once", choices=["chosen", "plain"], default=None,
+                    help="set up (train, autotune), then run one query of that form between "
+                         "cudaProfilerStart/Stop and exit (for ncu --profile-from-start off)")
     return ap.parse_args()
 
 
@@ -296,8 +297,13 @@ def main():
     else:
         chosen_kw = dict(flags=_lib.QF_AUTOTUNE)
     if args.profile_once:
-        index.batch_knn(query, k, **chosen_kw)
+        kw = chosen_kw if args.profile_once == "chosen" else plain_kw
+        index.batch_knn(query, k, **kw)  # autotunes on the first chosen-form call
         torch.cuda.synchronize(dev)
+        torch.cuda.profiler.start()
+        index.batch_knn(query, k, **kw)
+        torch.cuda.synchronize(dev)
+        torch.cuda.profiler.stop()
         index.close()
         return
 
@@ -347,7 +353,8 @@ def main():
     _lib.check(lib.knn_tuned_plan(index.handle, k, int(learned), ctypes.byref(tuned), ctypes.byref(tuned_ms)))
     tuned_plan = dict(block_size=tuned.block_size, heap=bool(tuned.heap_tracking),
                       shmem_tracking=bool(tuned.shmem_tracking), shmem_stack=bool(tuned.shmem_stack),
-                      leaf_scan=tuned.leaf_scan, candidates_timed=tuned.reserved[0])
+                      leaf_scan=tuned.leaf_scan, traversal="warp" if tuned.traversal else "thread",
+                      candidates_timed=tuned.reserved)
 
     with ClockSampler(local) as clocks:
         chosen_ms, chosen_kern_ms, launches = timed(chosen_kw, args.steps, args.warmup)

@@ -38,7 +38,7 @@ class QueryOpts(ctypes.Structure):
     _fields_ = [("block_size", ctypes.c_uint32), ("heap_tracking", ctypes.c_uint32),
                 ("shmem_tracking", ctypes.c_uint32), ("shmem_stack", ctypes.c_uint32),
                 ("flags", ctypes.c_uint32), ("leaf_scan", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 2)]
+                ("traversal", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class QueryCounters(ctypes.Structure):
@@ -98,6 +98,7 @@ _SIGNATURES = {
     "knn_radius_model_gradients": [_vp, _u32, _vp, _vp, _u32, _vp, _vp],
     "knn_last_query_timing": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
     "knn_launch_count": [],
+    "knn_tc_selftest": [_u32, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint32)],
     "knn_tuned_plan": [_vp, _u32, _u32, ctypes.POINTER(QueryOpts), ctypes.POINTER(ctypes.c_float)],
     "knn_status_string": [ctypes.c_int],
     "knn_last_error": [],
@@ -142,8 +143,11 @@ def check(status: int) -> None:
                        lib.knn_status_string(status).decode())
 
 
-def opts(block_size=0, heap=False, shmem_tracking=False, shmem_stack=False, flags=0, leaf_scan=0) -> QueryOpts:
+def opts(block_size=0, heap=False, shmem_tracking=False, shmem_stack=False, flags=0, leaf_scan=0,
+         traversal=0, tc_cap=0) -> QueryOpts:
     o = QueryOpts()
+    o.traversal = traversal
+    o.reserved = tc_cap
     o.block_size = block_size
     o.heap_tracking = int(bool(heap))
     o.shmem_tracking = int(bool(shmem_tracking))

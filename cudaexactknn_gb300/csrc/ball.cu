@@ -26,6 +26,8 @@ namespace knn {
 
 template <uint32_t DP>
 int ball_query_dp(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
+template <uint32_t DP>
+int ball_order_dp(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
 void leaf_layout(uint32_t dp, uint32_t* stride, uint32_t* id_at);
 
 namespace {
@@ -298,6 +300,21 @@ int ball_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream
         case 32: return ball_query_dp<32>(ix, a, p, s);
         case 64: return ball_query_dp<64>(ix, a, p, s);
         case 128: return ball_query_dp<128>(ix, a, p, s);
+        default: return fail(KNN_ERR_UNSUPPORTED, "dims %u", ix->dims);
+    }
+}
+
+int ball_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order) {
+    switch (ix->dp) {
+        case 1: return ball_order_dp<1>(ix, a, s, order);
+        case 2: return ball_order_dp<2>(ix, a, s, order);
+        case 3: return ball_order_dp<3>(ix, a, s, order);
+        case 4: return ball_order_dp<4>(ix, a, s, order);
+        case 8: return ball_order_dp<8>(ix, a, s, order);
+        case 16: return ball_order_dp<16>(ix, a, s, order);
+        case 32: return ball_order_dp<32>(ix, a, s, order);
+        case 64: return ball_order_dp<64>(ix, a, s, order);
+        case 128: return ball_order_dp<128>(ix, a, s, order);
         default: return fail(KNN_ERR_UNSUPPORTED, "dims %u", ix->dims);
     }
 }

@@ -137,6 +137,86 @@ __global__ void __launch_bounds__(256) ball_knn_kernel(const BallParams p) {
     }
 }
 
+// Warp-coherent variant (see kd_knn_warp_kernel): the warp's queries walk the tree together,
+// descending first into the child most still-interested lanes are closer to; each lane's bound
+// for a child is max(its inherited bound, its rigorous bound to the child's ball).
+template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
+__global__ void __launch_bounds__(256) ball_knn_warp_kernel(const BallParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t live = p.count_dev ? *p.count_dev : p.nq;
+    if ((t & ~31u) >= live) return;
+    const bool active = t < live;
+    uint64_t* sh_nn = reinterpret_cast<uint64_t*>(smem);
+    uint32_t* sh_st = reinterpret_cast<uint32_t*>(smem + tracker_smem_bytes(SHNN, KMAX, blockDim.x));
+
+    const uint32_t qi = active ? (p.order ? p.order[t] : t) : 0u;
+    float q[DP];
+    load_query<DP>(p.queries, p.dims, qi, q);
+    const float r2 = active ? (p.radii ? p.radii[qi] : p.max_d2) : 0.0f;
+
+    Tracker<KMAX, HEAP, SHNN> tr;
+    tr.init(p.k, r2, sh_nn + threadIdx.x, blockDim.x);
+    Stack<SHST> st;
+    st.init(sh_st, blockDim.x);
+    st.push(0, active ? 0.0f : INFINITY);
+    LocalCounters lc;
+    bool overflow = false;
+
+    while (st.top) {
+        uint32_t node;
+        float bound;
+        st.pop(&node, &bound);
+        if (!__any_sync(0xFFFFFFFFu, bound <= tr.radius())) continue;
+        uint32_t depth = heap_depth(node);
+        bool pruned = false;
+        while (depth < p.stop_depth) {
+            const uint32_t l = 2 * node + 1;
+            float rl, rr;
+            const float sl = centre_dist<DP>(q, p.ball + static_cast<size_t>(l) * p.ball_stride, &rl);
+            const float sr = centre_dist<DP>(q, p.ball + static_cast<size_t>(l + 1) * p.ball_stride, &rr);
+            const float bl = fmaxf(bound, ball_bound(sl, rl, p.margin));
+            const float br = fmaxf(bound, ball_bound(sr, rr, p.margin));
+            const bool want = bound <= tr.radius();
+            const bool left_near = sqrtf(sl) - rl < sqrtf(sr) - rr;
+            const uint32_t left_votes = __popc(__ballot_sync(0xFFFFFFFFu, want && left_near));
+            const uint32_t right_votes = __popc(__ballot_sync(0xFFFFFFFFu, want && !left_near));
+            const bool first_left = left_votes >= right_votes;
+            const float b_first = first_left ? bl : br;
+            const float b_second = first_left ? br : bl;
+            ++lc.nodes;
+            if (__any_sync(0xFFFFFFFFu, b_second <= tr.radius())) overflow |= !st.push(first_left ? l + 1 : l, b_second);
+            node = first_left ? l : l + 1;
+            bound = b_first;
+            ++depth;
+            if (!__any_sync(0xFFFFFFFFu, bound <= tr.radius())) {
+                pruned = true;
+                break;
+            }
+        }
+        if (pruned) continue;
+        const SlotRange r = subtree_slots(node, depth, p.node_depth, p.node_count, p.leaf_slots);
+        const float* slot = p.leaf + r.first * p.leaf_stride;
+        const bool want = bound <= tr.radius();
+        lc.leaves += want ? 1u : 0u;
+        for (uint32_t s = 0; s < r.count; ++s, slot += p.leaf_stride) {
+            int32_t id;
+            const float d2 = slot_dist<DP>(q, slot, &id);
+            if (id < 0) continue;
+            if (want) {
+                ++lc.points;
+                tr.offer(make_key(d2, id));
+            }
+        }
+    }
+    if (!active) return;
+    tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
+    if (p.counters) {
+        lc.flush(p.counters);
+        if (overflow) atomicExch(&p.counters->error, 1);
+    }
+}
+
 // Sort key of a query: the node reached after `levels` steps towards the nearer child centre.
 template <int DP>
 __global__ void ball_leaf_key_kernel(const float* __restrict__ ball, uint32_t ball_stride, uint32_t levels,
@@ -163,7 +243,7 @@ static int launch_ball(knn_index* ix, const QueryArgs& a, const QueryPlan& plan,
                        cudaStream_t s) {
     const uint32_t block = plan.block ? plan.block : 128;
     const size_t smem = tracker_smem_bytes(SHNN, KMAX, block) + stack_smem_bytes(SHST, block);
-    auto kern = ball_knn_kernel<DP, KMAX, HEAP, SHNN, SHST>;
+    auto kern = plan.warp ? ball_knn_warp_kernel<DP, KMAX, HEAP, SHNN, SHST> : ball_knn_kernel<DP, KMAX, HEAP, SHNN, SHST>;
     if (smem > 48 * 1024)
         KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     BallParams p{};
@@ -212,27 +292,36 @@ static int launch_ball_variant(knn_index* ix, const QueryArgs& a, const QueryPla
     return fail(KNN_ERR_INVALID_ARGUMENT, "bad query plan");
 }
 
+// Query order for locality: queries sorted by the node they reach after up to 24 greedy
+// descent steps (stable radix sort on the path bits).  The order lives in the index workspace
+// until the next query.
+template <uint32_t DP>
+int ball_order_dp(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order) {
+    *order = nullptr;
+    const uint32_t levels = std::min<uint32_t>(ix->node_depth, 24);
+    if (levels == 0) return KNN_OK;
+    const size_t nq = a.count;
+    const size_t need = carve_bytes({nq * 4, nq * 4, nq * 4, nq * 4, radix_sort_temp_bytes(a.count)});
+    KNN_TRY(ix->workspace.reserve(need));
+    Carver c(ix->workspace.ptr);
+    uint32_t* keys = c.take<uint32_t>(nq);
+    uint32_t* vals = c.take<uint32_t>(nq);
+    uint32_t* keys_alt = c.take<uint32_t>(nq);
+    uint32_t* vals_alt = c.take<uint32_t>(nq);
+    void* temp = c.take<uint8_t>(radix_sort_temp_bytes(a.count));
+    ball_leaf_key_kernel<DP><<<ceil_div(a.count, 256), 256, 0, s>>>(ix->ball.as<float>(), ix->ball_stride, levels,
+                                                       a.queries, ix->dims, a.count, keys, vals);
+    KNN_LAUNCHED();
+    bool in_alt = false;
+    KNN_TRY(radix_sort_pairs(keys, vals, keys_alt, vals_alt, a.count, static_cast<int>(levels), temp, s, &in_alt));
+    *order = in_alt ? vals_alt : vals;
+    return KNN_OK;
+}
+
 template <uint32_t DP>
 int ball_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s) {
     const uint32_t* order = a.order;
-    const uint32_t levels = std::min<uint32_t>(ix->node_depth, 24);
-    if (!order && p.reorder && a.count >= 4096 && levels > 0) {
-        const size_t nq = a.count;
-        const size_t need = carve_bytes({nq * 4, nq * 4, nq * 4, nq * 4, radix_sort_temp_bytes(a.count)});
-        KNN_TRY(ix->workspace.reserve(need));
-        Carver c(ix->workspace.ptr);
-        uint32_t* keys = c.take<uint32_t>(nq);
-        uint32_t* vals = c.take<uint32_t>(nq);
-        uint32_t* keys_alt = c.take<uint32_t>(nq);
-        uint32_t* vals_alt = c.take<uint32_t>(nq);
-        void* temp = c.take<uint8_t>(radix_sort_temp_bytes(a.count));
-        ball_leaf_key_kernel<DP><<<ceil_div(a.count, 256), 256, 0, s>>>(ix->ball.as<float>(), ix->ball_stride, levels,
-                                                                        a.queries, ix->dims, a.count, keys, vals);
-        KNN_LAUNCHED();
-        bool in_alt = false;
-        KNN_TRY(radix_sort_pairs(keys, vals, keys_alt, vals_alt, a.count, static_cast<int>(levels), temp, s, &in_alt));
-        order = in_alt ? vals_alt : vals;
-    }
+    if (!order && p.reorder && a.count >= 4096) KNN_TRY(ball_order_dp<DP>(ix, a, s, &order));
     switch (k_class(a.k)) {
         case 8: return launch_ball_variant<DP, 8>(ix, a, p, order, s);
         case 16: return launch_ball_variant<DP, 16>(ix, a, p, order, s);
@@ -243,5 +332,6 @@ int ball_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStr
 }
 
 template int ball_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
+template int ball_order_dp<KNN_DP>(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
 
 }  // namespace knn

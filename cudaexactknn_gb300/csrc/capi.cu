@@ -111,7 +111,11 @@ int make_plan(const knn_index* ix, const knn_query_opts* o, knn::QueryPlan* p) {
     p->sh_stack = o->shmem_stack != 0;
     p->reorder = (o->flags & KNN_QF_KEEP_ORDER) == 0;
     p->timing = (o->flags & KNN_QF_TIMING) != 0;
+    p->bf16 = (o->flags & KNN_QF_BF16_FILTER) != 0 && ix->structure == KNN_BRUTE_FORCE;
+    p->tc_cap = o->reserved;
     p->leaf_scan = o->leaf_scan;
+    if (o->traversal > 1) return fail(KNN_ERR_INVALID_ARGUMENT, "traversal %u: 0 or 1", o->traversal);
+    p->warp = o->traversal == 1;
     (void)ix;
     return KNN_OK;
 }
@@ -126,28 +130,45 @@ int dispatch(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& plan,
     }
 }
 
-// Learned radius: seed each query's radius from the model, search, collect the queries that
-// found fewer than k points inside a seed below the caller's radius, and search those again
-// with the caller's radius.  Results are exact either way.
+// Learned radius: seed each query's radius from the model and search.  Queries that found fewer
+// than k points inside a seed below the caller's radius are searched again with the radius
+// grown 16x (squared distance), twice, and then with the caller's radius, which makes every
+// answer exact.  Retry lists keep the locality order of the batch.
+constexpr int kSeedRounds = 3;
+constexpr float kSeedGrowth = 16.0f;
+
 int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& plan, cudaStream_t s) {
     const size_t n = a.count;
-    KNN_TRY(ix->seed_ws.reserve(knn::carve_bytes({n * 4, n * 4, 256})));
+    const uint32_t* order = nullptr;
+    if (plan.reorder && a.count >= 4096) {
+        if (ix->structure == KNN_KD_TREE) KNN_TRY(knn::kd_order(ix, a, s, &order));
+        if (ix->structure == KNN_BALL_TREE) KNN_TRY(knn::ball_order(ix, a, s, &order));
+    }
+    KNN_TRY(ix->seed_ws.reserve(knn::carve_bytes({n * 4, n * 4, 256, knn::retry_scratch_bytes(a.count)})));
     knn::Carver c(ix->seed_ws.ptr);
     float* radii = c.take<float>(n);
     uint32_t* list = c.take<uint32_t>(n);
     uint32_t* list_count = c.take<uint32_t>(1);
+    void* scratch = c.take<uint8_t>(knn::retry_scratch_bytes(a.count));
     KNN_TRY(knn::model_predict(ix->model.as<float>(), ix->dims, a.queries, a.count, a.max_d2, a.radii, radii,
                                nullptr, s));
     knn::QueryArgs seeded = a;
     seeded.radii = radii;
+    seeded.order = order;
     KNN_TRY(dispatch(ix, seeded, plan, s));
-    KNN_TRY(knn::model_fallbacks(a.out_idx, a.count, a.k, radii, a.max_d2, a.radii, list, list_count, a.counters, s));
-    knn::QueryArgs again = a;
-    again.order = list;
-    again.count_dev = list_count;
-    knn::QueryPlan plain = plan;
-    plain.timing = false;  // the timed kernel span stays the seeded search
-    return dispatch(ix, again, plain, s);
+    knn::QueryPlan again_plan = plan;
+    again_plan.timing = false;  // the timed kernel span stays the seeded search
+    for (int round = 0; round < kSeedRounds; ++round) {
+        const float grow = round + 1 < kSeedRounds ? kSeedGrowth : INFINITY;
+        KNN_TRY(knn::model_retry_list(order, a.out_idx, a.count, a.k, radii, a.max_d2, a.radii, grow, list,
+                                      list_count, scratch, round == 0 ? a.counters : nullptr, s));
+        knn::QueryArgs again = a;
+        again.radii = radii;
+        again.order = list;
+        again.count_dev = list_count;
+        KNN_TRY(dispatch(ix, again, again_plan, s));
+    }
+    return KNN_OK;
 }
 
 int k_slot(uint32_t k) {
@@ -204,11 +225,15 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
     };
     do {
         if (ix->structure != KNN_BRUTE_FORCE) {
-            for (uint32_t leaf : {0u, 4u, 8u, 16u, 32u, 64u}) {
-                if (leaf && leaf <= ix->leaf_slots) continue;
-                knn::QueryPlan p = best;
-                p.leaf_scan = leaf;
-                if ((rc = consider(p)) != KNN_OK) break;
+            for (bool warp : {false, true}) {
+                for (uint32_t leaf : {0u, 4u, 8u, 16u, 32u, 64u}) {
+                    if (leaf && leaf <= ix->leaf_slots) continue;
+                    knn::QueryPlan p = best;
+                    p.warp = warp;
+                    p.leaf_scan = leaf;
+                    if ((rc = consider(p)) != KNN_OK) break;
+                }
+                if (rc != KNN_OK) break;
             }
             if (rc != KNN_OK) break;
         } else if ((rc = consider(best)) != KNN_OK) {
@@ -447,9 +472,16 @@ int knn_tuned_plan(const knn_index* index, uint32_t k, uint32_t learned_radius, 
     out->shmem_tracking = slot.plan.sh_nn;
     out->shmem_stack = slot.plan.sh_stack;
     out->leaf_scan = slot.plan.leaf_scan;
-    out->reserved[0] = slot.candidates;
+    out->traversal = slot.plan.warp ? 1u : 0u;
+    out->reserved = slot.candidates;
     if (ms) *ms = slot.ms;
     return KNN_OK;
+}
+
+int knn_tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* mismatches) {
+    if (!max_rel_err || !mismatches) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
+    if (dims == 0 || dims > 128) return fail(KNN_ERR_UNSUPPORTED, "dims %u", dims);
+    return knn::tc_selftest(dims, max_rel_err, mismatches);
 }
 
 uint64_t knn_launch_count(void) { return knn::g_launches.load(); }
@@ -462,7 +494,7 @@ int knn_radius_model_train(knn_index* index, const float* d_samples, uint32_t co
     if (k == 0 || k > knn::kMaxK) return fail(k ? KNN_ERR_UNSUPPORTED : KNN_ERR_INVALID_ARGUMENT, "k %u", k);
     knn_train_opts o{};
     if (opts) o = *opts;
-    if (!o.steps) o.steps = 1500;
+    if (!o.steps) o.steps = 3000;
     if (!o.batch) o.batch = 1024;
     if (!(o.lr > 0.0f)) o.lr = 3e-3f;
     if (!(o.coverage > 0.0f && o.coverage < 1.0f)) o.coverage = 0.98f;
@@ -522,7 +554,7 @@ int knn_radius_model_gradients(const float* h_params, uint32_t dims, const float
     KNN_TRY_CUDA(cudaMemcpy(x, h_x, static_cast<size_t>(batch) * dims * 4, cudaMemcpyHostToDevice));
     KNN_TRY_CUDA(cudaMemcpy(t, h_targets, static_cast<size_t>(batch) * 4, cudaMemcpyHostToDevice));
     KNN_TRY(knn::model_gradients(prm, dims, x, t, nullptr, batch, grad, loss, scratch, nullptr));
-    const size_t trainable = np - 2 * dims - 1;
+    const size_t trainable = np - dims * 32 - 2 * dims - 1;  // fixed projection, scaling, margin follow
     KNN_TRY_CUDA(cudaMemcpy(h_grad, grad, trainable * 4, cudaMemcpyDeviceToHost));
     std::vector<float> lr(batch);
     KNN_TRY_CUDA(cudaMemcpy(lr.data(), loss, static_cast<size_t>(batch) * 4, cudaMemcpyDeviceToHost));

@@ -17,6 +17,8 @@ namespace knn {
 
 template <uint32_t DP>
 int kd_query_dp(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
+template <uint32_t DP>
+int kd_order_dp(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
 
 namespace {
 
@@ -136,6 +138,21 @@ int kd_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t
         case 32: return kd_query_dp<32>(ix, a, p, s);
         case 64: return kd_query_dp<64>(ix, a, p, s);
         case 128: return kd_query_dp<128>(ix, a, p, s);
+        default: return fail(KNN_ERR_UNSUPPORTED, "dims %u", ix->dims);
+    }
+}
+
+int kd_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order) {
+    switch (ix->dp) {
+        case 1: return kd_order_dp<1>(ix, a, s, order);
+        case 2: return kd_order_dp<2>(ix, a, s, order);
+        case 3: return kd_order_dp<3>(ix, a, s, order);
+        case 4: return kd_order_dp<4>(ix, a, s, order);
+        case 8: return kd_order_dp<8>(ix, a, s, order);
+        case 16: return kd_order_dp<16>(ix, a, s, order);
+        case 32: return kd_order_dp<32>(ix, a, s, order);
+        case 64: return kd_order_dp<64>(ix, a, s, order);
+        case 128: return kd_order_dp<128>(ix, a, s, order);
         default: return fail(KNN_ERR_UNSUPPORTED, "dims %u", ix->dims);
     }
 }

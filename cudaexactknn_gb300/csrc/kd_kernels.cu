@@ -100,6 +100,94 @@ __global__ void __launch_bounds__(256) kd_knn_kernel(const KdParams p) {
     }
 }
 
+// Warp-coherent variant: the 32 queries of a warp (neighbours after the leaf-order sort) walk the
+// tree together.  Each node's split is one broadcast load; the warp descends first into the
+// child most of its still-interested lanes are closer to; every lane keeps its own lower bound
+// for each stacked subtree, max(bound inherited from the parent, its squared distance to the
+// plane), and a subtree is skipped only when no lane's bound is within that lane's radius.
+// Leaf buckets are scanned by all lanes against the same slots (broadcast loads).  Control flow
+// is uniform across the warp; only the (rare) top-k insertions diverge.
+template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
+__global__ void __launch_bounds__(256) kd_knn_warp_kernel(const KdParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t live = p.count_dev ? *p.count_dev : p.nq;
+    const uint32_t warp_first = t & ~31u;
+    if (warp_first >= live) return;  // whole warp idle; no block-wide barriers below
+    const bool active = t < live;
+    uint64_t* sh_nn = reinterpret_cast<uint64_t*>(smem);
+    uint32_t* sh_st = reinterpret_cast<uint32_t*>(smem + tracker_smem_bytes(SHNN, KMAX, blockDim.x));
+
+    const uint32_t qi = active ? (p.order ? p.order[t] : t) : 0u;
+    float q[DP];
+    load_query<DP>(p.queries, p.dims, qi, q);
+    // Idle lanes (past the end of the batch) search with radius -1: they never want a node.
+    const float r2 = active ? (p.radii ? p.radii[qi] : p.max_d2) : 0.0f;
+
+    Tracker<KMAX, HEAP, SHNN> tr;
+    tr.init(p.k, r2, sh_nn + threadIdx.x, blockDim.x);
+    Stack<SHST> st;
+    st.init(sh_st, blockDim.x);
+    st.push(0, active ? 0.0f : INFINITY);
+    LocalCounters lc;
+    bool overflow = false;
+
+    while (st.top) {  // st.top is warp-uniform: every lane pushes and pops together
+        uint32_t node;
+        float bound;
+        st.pop(&node, &bound);
+        if (!__any_sync(0xFFFFFFFFu, bound <= tr.radius())) continue;
+        uint32_t depth = heap_depth(node);
+        bool pruned = false;
+        while (depth < p.stop_depth) {
+            const uint32_t dim = depth % p.aux;
+            const float diff = __fsub_rn(pick<DP>(q, dim), __ldg(p.split + node));
+            const float b = fmaxf(bound, __fmul_rn(diff, diff));
+            const bool want = bound <= tr.radius();
+            const bool go_left = diff < 0.0f;
+            const uint32_t left_votes = __popc(__ballot_sync(0xFFFFFFFFu, want && go_left));
+            const uint32_t right_votes = __popc(__ballot_sync(0xFFFFFFFFu, want && !go_left));
+            const bool first_left = left_votes >= right_votes;
+            const uint32_t l = 2 * node + 1;
+            // This lane's bound for each child: its inherited bound on its own side, the plane
+            // bound on the other.
+            const float b_left = go_left ? bound : b;
+            const float b_right = go_left ? b : bound;
+            const float b_first = first_left ? b_left : b_right;
+            const float b_second = first_left ? b_right : b_left;
+            ++lc.nodes;
+            if (__any_sync(0xFFFFFFFFu, b_second <= tr.radius())) overflow |= !st.push(first_left ? l + 1 : l, b_second);
+            node = first_left ? l : l + 1;
+            bound = b_first;
+            ++depth;
+            if (!__any_sync(0xFFFFFFFFu, bound <= tr.radius())) {
+                pruned = true;
+                break;
+            }
+        }
+        if (pruned) continue;
+        const SlotRange r = subtree_slots(node, depth, p.node_depth, p.node_count, p.leaf_slots);
+        const float* slot = p.leaf + r.first * p.leaf_stride;
+        const bool want = bound <= tr.radius();
+        lc.leaves += want ? 1u : 0u;
+        for (uint32_t s = 0; s < r.count; ++s, slot += p.leaf_stride) {
+            int32_t id;
+            const float d2 = slot_dist<DP>(q, slot, &id);
+            if (id < 0) continue;
+            if (want) {
+                ++lc.points;
+                tr.offer(make_key(d2, id));
+            }
+        }
+    }
+    if (!active) return;
+    tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
+    if (p.counters) {
+        lc.flush(p.counters);
+        if (overflow) atomicExch(&p.counters->error, 1);
+    }
+}
+
 // Sort key of a query: the node it reaches after `levels` closer-child steps (path bits).
 template <int DP>
 __global__ void kd_leaf_key_kernel(const float* __restrict__ split, uint32_t aux, uint32_t levels,
@@ -123,7 +211,7 @@ static int launch_kd(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, c
                      cudaStream_t s) {
     const uint32_t block = plan.block ? plan.block : 128;
     const size_t smem = tracker_smem_bytes(SHNN, KMAX, block) + stack_smem_bytes(SHST, block);
-    auto kern = kd_knn_kernel<DP, KMAX, HEAP, SHNN, SHST>;
+    auto kern = plan.warp ? kd_knn_warp_kernel<DP, KMAX, HEAP, SHNN, SHST> : kd_knn_kernel<DP, KMAX, HEAP, SHNN, SHST>;
     if (smem > 48 * 1024)
         KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     KdParams p{};
@@ -171,27 +259,36 @@ static int launch_kd_variant(knn_index* ix, const QueryArgs& a, const QueryPlan&
     return fail(KNN_ERR_INVALID_ARGUMENT, "bad query plan");
 }
 
+// Query order for locality: queries sorted by the node they reach after up to 24 greedy
+// descent steps (stable radix sort on the path bits).  The order lives in the index workspace
+// until the next query.
+template <uint32_t DP>
+int kd_order_dp(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order) {
+    *order = nullptr;
+    const uint32_t levels = std::min<uint32_t>(ix->node_depth, 24);
+    if (levels == 0) return KNN_OK;
+    const size_t nq = a.count;
+    const size_t need = carve_bytes({nq * 4, nq * 4, nq * 4, nq * 4, radix_sort_temp_bytes(a.count)});
+    KNN_TRY(ix->workspace.reserve(need));
+    Carver c(ix->workspace.ptr);
+    uint32_t* keys = c.take<uint32_t>(nq);
+    uint32_t* vals = c.take<uint32_t>(nq);
+    uint32_t* keys_alt = c.take<uint32_t>(nq);
+    uint32_t* vals_alt = c.take<uint32_t>(nq);
+    void* temp = c.take<uint8_t>(radix_sort_temp_bytes(a.count));
+    kd_leaf_key_kernel<DP><<<ceil_div(a.count, 256), 256, 0, s>>>(ix->split.as<float>(), ix->aux_dims, levels,
+                                                       a.queries, ix->dims, a.count, keys, vals);
+    KNN_LAUNCHED();
+    bool in_alt = false;
+    KNN_TRY(radix_sort_pairs(keys, vals, keys_alt, vals_alt, a.count, static_cast<int>(levels), temp, s, &in_alt));
+    *order = in_alt ? vals_alt : vals;
+    return KNN_OK;
+}
+
 template <uint32_t DP>
 int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s) {
     const uint32_t* order = a.order;
-    const uint32_t levels = std::min<uint32_t>(ix->node_depth, 24);
-    if (!order && p.reorder && a.count >= 4096 && levels > 0) {
-        const size_t nq = a.count;
-        const size_t need = carve_bytes({nq * 4, nq * 4, nq * 4, nq * 4, radix_sort_temp_bytes(a.count)});
-        KNN_TRY(ix->workspace.reserve(need));
-        Carver c(ix->workspace.ptr);
-        uint32_t* keys = c.take<uint32_t>(nq);
-        uint32_t* vals = c.take<uint32_t>(nq);
-        uint32_t* keys_alt = c.take<uint32_t>(nq);
-        uint32_t* vals_alt = c.take<uint32_t>(nq);
-        void* temp = c.take<uint8_t>(radix_sort_temp_bytes(a.count));
-        kd_leaf_key_kernel<DP><<<ceil_div(a.count, 256), 256, 0, s>>>(ix->split.as<float>(), ix->aux_dims, levels,
-                                                                      a.queries, ix->dims, a.count, keys, vals);
-        KNN_LAUNCHED();
-        bool in_alt = false;
-        KNN_TRY(radix_sort_pairs(keys, vals, keys_alt, vals_alt, a.count, static_cast<int>(levels), temp, s, &in_alt));
-        order = in_alt ? vals_alt : vals;
-    }
+    if (!order && p.reorder && a.count >= 4096) KNN_TRY(kd_order_dp<DP>(ix, a, s, &order));
     switch (k_class(a.k)) {
         case 8: return launch_kd_variant<DP, 8>(ix, a, p, order, s);
         case 16: return launch_kd_variant<DP, 16>(ix, a, p, order, s);
@@ -202,5 +299,6 @@ int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStrea
 }
 
 template int kd_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
+template int kd_order_dp<KNN_DP>(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
 
 }  // namespace knn

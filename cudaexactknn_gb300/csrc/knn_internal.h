@@ -135,6 +135,9 @@ struct QueryPlan {
     bool sh_stack = false;
     bool reorder = true;
     bool timing = false;     // record events around the main search kernel
+    bool warp = false;       // trees: warp-coherent traversal instead of one search per thread
+    bool bf16 = false;       // brute force: BF16 tensor-core filter + FP32 rescoring
+    uint32_t tc_cap = 0;     // candidates kept per query by the filter (0 = default)
     uint32_t leaf_scan = 0;  // 0 = tree leaves
 };
 
@@ -164,6 +167,11 @@ struct knn_index {
     // Brute force: points, padded to `point_stride` floats (a multiple of 4), zero padding.
     knn::DevBuf points;
     uint32_t point_stride = 0;
+
+    // Brute force, tensor-core filter: BF16 point image (128-byte swizzle tiles of 256 points)
+    // and {|p|^2, |p|} per point, built on first use; scratch for the query images and candidates.
+    knn::DevBuf tc_img, tc_norm, tc_ws;
+    bool tc_ready = false;
 
     // k-d tree: split value per internal node (implicit heap, children 2i+1, 2i+2).
     knn::DevBuf split;
@@ -241,13 +249,24 @@ int model_gradients(const float* d_prm, uint32_t dims, const float* d_x, const f
                     uint32_t batch, float* d_grad, float* d_loss_rows, DevBuf& scratch, cudaStream_t s);
 int model_predict(const float* d_prm, uint32_t dims, const float* d_x, uint32_t count, float max_d2,
                   const float* user_radii, float* d_radii, float* d_raw, cudaStream_t s);
-int model_fallbacks(const int32_t* out_idx, uint32_t count, uint32_t k, const float* seeded, float max_d2,
-                    const float* user_radii, uint32_t* list, uint32_t* list_count, DevCounters* counters,
-                    cudaStream_t s);
+// Stable list (in `order`, or index order) of the queries that must be searched again, with
+// their seeded radii grown by `grow` (capped by the caller's radius).
+size_t retry_scratch_bytes(uint32_t count);
+int model_retry_list(const uint32_t* order, const int32_t* out_idx, uint32_t count, uint32_t k, float* seeded,
+                     float max_d2, const float* user_radii, float grow, uint32_t* list, uint32_t* list_count,
+                     void* scratch, DevCounters* counters, cudaStream_t s);
 int model_train(knn_index* ix, const float* d_samples, uint32_t count, uint32_t k, const knn_train_opts& o,
                 cudaStream_t s, knn_train_report* rep);
 
 int bf_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
+// Brute force through the BF16 tensor-core filter (bf_tc.cu).
+bool tc_supported(uint32_t dims, uint32_t k);
+int tc_prepare(knn_index* ix, cudaStream_t s);
+int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
+int tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* bad);
+// Locality order of a query batch for the trees (kd_order / ball_order), in the index workspace.
+int kd_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order);
+int ball_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order);
 int kd_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 int ball_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 

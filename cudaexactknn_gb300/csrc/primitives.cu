@@ -96,42 +96,58 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     }
 }
 
-// Exclusive scan of each row of a [rows][cols] u32 matrix; one block of 1024 threads per row,
-// each thread owning a contiguous chunk.
+// Exclusive scan of each row of a [rows][cols] u32 matrix; one block of 1024 threads per row.
+// The row streams through shared memory in coalesced tiles of 4096 entries with a running carry.
 __global__ void __launch_bounds__(1024) scan_rows_kernel(const uint32_t* __restrict__ in,
                                                          uint32_t* __restrict__ out, uint32_t cols) {
+    constexpr uint32_t kT = 1024, kTile = 4 * kT;
+    __shared__ uint32_t tile[kTile];
     __shared__ uint32_t warp_sums[32];
     const uint32_t* row_in = in + static_cast<size_t>(blockIdx.x) * cols;
     uint32_t* row_out = out + static_cast<size_t>(blockIdx.x) * cols;
-    const uint32_t chunk = (cols + blockDim.x - 1) / blockDim.x;
-    const uint32_t lo = min(cols, threadIdx.x * chunk), hi = min(cols, lo + chunk);
-    uint32_t sum = 0;
-    for (uint32_t i = lo; i < hi; ++i) sum += row_in[i];
-    // Block-wide exclusive scan of the per-thread sums.
-    const uint32_t lane = threadIdx.x % 32, warp = threadIdx.x / 32;
-    uint32_t incl = sum;
+    const uint32_t tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < cols; base += kTile) {
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= static_cast<uint32_t>(o)) incl += v;
-    }
-    if (lane == 31) warp_sums[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = lane < blockDim.x / 32 ? warp_sums[lane] : 0;
+        for (uint32_t i = 0; i < 4; ++i) {
+            const uint32_t idx = base + i * kT + tid;
+            tile[i * kT + tid] = idx < cols ? row_in[idx] : 0u;
+        }
+        __syncthreads();
+        const uint32_t a = tile[4 * tid], b = tile[4 * tid + 1], c = tile[4 * tid + 2], d = tile[4 * tid + 3];
+        const uint32_t sum = a + b + c + d;
+        uint32_t incl = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, w, o);
-            if (lane >= static_cast<uint32_t>(o)) w += v;
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<uint32_t>(o)) incl += v;
         }
-        warp_sums[lane] = w;  // inclusive over warps
-    }
-    __syncthreads();
-    uint32_t run = incl - sum + (warp > 0 ? warp_sums[warp - 1] : 0);
-    for (uint32_t i = lo; i < hi; ++i) {
-        const uint32_t v = row_in[i];
-        row_out[i] = run;
-        run += v;
+        if (lane == 31) warp_sums[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = warp_sums[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, w, o);
+                if (lane >= static_cast<uint32_t>(o)) w += v;
+            }
+            warp_sums[lane] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        const uint32_t excl = carry + incl - sum + (warp > 0 ? warp_sums[warp - 1] : 0u);
+        tile[4 * tid] = excl;
+        tile[4 * tid + 1] = excl + a;
+        tile[4 * tid + 2] = excl + a + b;
+        tile[4 * tid + 3] = excl + a + b + c;
+        const uint32_t tile_total = warp_sums[31];
+        __syncthreads();
+#pragma unroll
+        for (uint32_t i = 0; i < 4; ++i) {
+            const uint32_t idx = base + i * kT + tid;
+            if (idx < cols) row_out[idx] = tile[i * kT + tid];
+        }
+        carry += tile_total;
+        __syncthreads();
     }
 }
 

@@ -10,8 +10,14 @@
 // caller's single Query::maxDistance2 (src/KnnTrees.cuh:228, used at src/KdTreeGpu.cuh:211 and
 // src/BallTreeGpu.cuh:48).
 //
-// Parameter layout (floats): W1[64][D] b1[64] W2[64][64] b2[64] w3[64] b3, then the input
-// normalisation mu[D] inv_sd[D] and the calibrated margin.
+// Input encoding: the coordinates scaled to [0, 1]^D (per-dimension range of the training
+// samples), followed by sin and cos of 32 fixed random projections 2 pi z . B (B ~ N(0, 4^2),
+// seeded): E = D + 64 features.  Fourier features of this kind (Tancik et al., NeurIPS 2020) let a
+// small ReLU network fit the narrow density peaks of clustered data; on raw coordinates the same
+// 64-64 network learned nothing beyond the mean for a 64-cluster mixture.
+//
+// Parameter layout (floats): W1[64][E] b1[64] W2[64][64] b2[64] w3[64] b3 (trainable), then the
+// fixed projection B[D][32], the scaling lo[D] inv_range[D], and the calibrated margin.
 
 #include <algorithm>
 #include <cmath>
@@ -24,24 +30,42 @@
 namespace knn {
 
 constexpr uint32_t kHidden = 64;
+constexpr uint32_t kFourier = 32;
+constexpr float kFourierScale = 4.0f;
 
 struct ModelLayout {
-    uint32_t dims;
-    uint32_t w1, b1, w2, b2, w3, b3, mu, inv_sd, margin, total, trainable;
-    __host__ __device__ explicit ModelLayout(uint32_t d) : dims(d) {
+    uint32_t dims, feats;
+    uint32_t w1, b1, w2, b2, w3, b3, proj, lo, inv_range, margin, total, trainable;
+    __host__ __device__ explicit ModelLayout(uint32_t d) : dims(d), feats(d + 2 * kFourier) {
         w1 = 0;
-        b1 = w1 + kHidden * d;
+        b1 = w1 + kHidden * feats;
         w2 = b1 + kHidden;
         b2 = w2 + kHidden * kHidden;
         w3 = b2 + kHidden;
         b3 = w3 + kHidden;
         trainable = b3 + 1;
-        mu = trainable;
-        inv_sd = mu + d;
-        margin = inv_sd + d;
+        proj = trainable;
+        lo = proj + d * kFourier;
+        inv_range = lo + d;
+        margin = inv_range + d;
         total = margin + 1;
     }
 };
+
+// Features of one input row: e[0..D) = scaled coordinates, e[D+f] = sin(2 pi z.B_f),
+// e[D+32+f] = cos(2 pi z.B_f).
+__device__ __forceinline__ void encode(const float* __restrict__ prm, const ModelLayout& L,
+                                       const float* __restrict__ x, float* __restrict__ e) {
+    for (uint32_t d = 0; d < L.dims; ++d) e[d] = (x[d] - prm[L.lo + d]) * prm[L.inv_range + d];
+    for (uint32_t f = 0; f < kFourier; ++f) {
+        float a = 0.0f;
+        for (uint32_t d = 0; d < L.dims; ++d) a = fmaf(e[d], prm[L.proj + d * kFourier + f], a);
+        float sv, cv;
+        sincosf(6.283185307179586f * a, &sv, &cv);
+        e[L.dims + f] = sv;
+        e[L.dims + kFourier + f] = cv;
+    }
+}
 
 namespace {
 
@@ -57,15 +81,12 @@ __global__ void mlp_fwd_bwd_kernel(const float* __restrict__ prm, uint32_t dims,
     if (b >= batch) return;
     const ModelLayout L(dims);
     const uint32_t r = rows ? rows[b] : b;
-    float xn[kMaxDims];
-    for (uint32_t d = 0; d < dims; ++d) {
-        xn[d] = (x[static_cast<size_t>(r) * dims + d] - prm[L.mu + d]) * prm[L.inv_sd + d];
-        xn_out[static_cast<size_t>(b) * dims + d] = xn[d];
-    }
+    float* xn = xn_out + static_cast<size_t>(b) * L.feats;  // the sample's features
+    encode(prm, L, x + static_cast<size_t>(r) * dims, xn);
     float h1[kHidden], h2[kHidden];
     for (uint32_t i = 0; i < kHidden; ++i) {
         float a = prm[L.b1 + i];
-        for (uint32_t d = 0; d < dims; ++d) a = fmaf(prm[L.w1 + i * dims + d], xn[d], a);
+        for (uint32_t d = 0; d < L.feats; ++d) a = fmaf(prm[L.w1 + i * L.feats + d], xn[d], a);
         h1[i] = fmaxf(a, 0.0f);
         h1_out[static_cast<size_t>(b) * kHidden + i] = h1[i];
     }
@@ -104,8 +125,8 @@ __global__ void mlp_grad_kernel(uint32_t dims, uint32_t batch, const float* __re
     if (p >= L.trainable) return;
     float g = 0.0f;
     if (p < L.b1) {
-        const uint32_t i = p / dims, d = p % dims;
-        for (uint32_t b = 0; b < batch; ++b) g = fmaf(d1[b * kHidden + i], xn[b * dims + d], g);
+        const uint32_t i = p / L.feats, d = p % L.feats;
+        for (uint32_t b = 0; b < batch; ++b) g = fmaf(d1[b * kHidden + i], xn[b * L.feats + d], g);
     } else if (p < L.w2) {
         const uint32_t i = p - L.b1;
         for (uint32_t b = 0; b < batch; ++b) g += d1[b * kHidden + i];
@@ -138,6 +159,71 @@ __global__ void adam_kernel(float* __restrict__ prm, const float* __restrict__ g
     prm[p] -= lr * (mp / corr1) / (sqrtf(vp / corr2) + eps);
 }
 
+// Seeded radius of each query, specialised on the padded input width: the parameters are
+// staged in shared memory (every thread reads the same weights: broadcast float4 loads), the
+// hidden activations stay in registers.
+template <int DP>
+__global__ void __launch_bounds__(256) mlp_infer_fast_kernel(const float* __restrict__ prm, uint32_t dims,
+                                                             const float* __restrict__ x, uint32_t count,
+                                                             float max_d2, const float* __restrict__ user_radii,
+                                                             float* __restrict__ radii, float* __restrict__ raw) {
+    extern __shared__ __align__(16) float sp[];
+    const ModelLayout L(dims);
+    for (uint32_t i = threadIdx.x; i < L.total; i += blockDim.x) sp[i] = prm[i];
+    __syncthreads();
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count) return;
+    float z[DP];
+#pragma unroll
+    for (int d = 0; d < DP; ++d)
+        z[d] = static_cast<uint32_t>(d) < dims ? (x[static_cast<size_t>(q) * dims + d] - sp[L.lo + d]) * sp[L.inv_range + d]
+                                               : 0.0f;
+    // First layer over the features, accumulated feature by feature.
+    float h1[kHidden];
+#pragma unroll
+    for (int i = 0; i < static_cast<int>(kHidden); ++i) h1[i] = sp[L.b1 + i];
+#pragma unroll
+    for (int d = 0; d < DP; ++d)
+        if (static_cast<uint32_t>(d) < dims)
+#pragma unroll
+            for (int i = 0; i < static_cast<int>(kHidden); ++i) h1[i] = fmaf(sp[L.w1 + i * L.feats + d], z[d], h1[i]);
+#pragma unroll 1
+    for (uint32_t f = 0; f < kFourier; ++f) {
+        float a = 0.0f;
+#pragma unroll
+        for (int d = 0; d < DP; ++d)
+            if (static_cast<uint32_t>(d) < dims) a = fmaf(z[d], sp[L.proj + d * kFourier + f], a);
+        float sv, cv;
+        sincosf(6.283185307179586f * a, &sv, &cv);
+#pragma unroll
+        for (int i = 0; i < static_cast<int>(kHidden); ++i) {
+            h1[i] = fmaf(sp[L.w1 + i * L.feats + dims + f], sv, h1[i]);
+            h1[i] = fmaf(sp[L.w1 + i * L.feats + dims + kFourier + f], cv, h1[i]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < static_cast<int>(kHidden); ++i) h1[i] = fmaxf(h1[i], 0.0f);
+    float y = sp[L.b3];
+    const float4* w2 = reinterpret_cast<const float4*>(sp + L.w2);  // W2 starts at a multiple of 4 floats
+    for (int i = 0; i < static_cast<int>(kHidden); ++i) {
+        float a = sp[L.b2 + i];
+#pragma unroll
+        for (int j4 = 0; j4 < static_cast<int>(kHidden / 4); ++j4) {
+            const float4 w = w2[i * (kHidden / 4) + j4];
+            a = fmaf(w.x, h1[4 * j4 + 0], a);
+            a = fmaf(w.y, h1[4 * j4 + 1], a);
+            a = fmaf(w.z, h1[4 * j4 + 2], a);
+            a = fmaf(w.w, h1[4 * j4 + 3], a);
+        }
+        y = fmaf(sp[L.w3 + i], fmaxf(a, 0.0f), y);
+    }
+    if (raw) raw[q] = y;
+    if (radii) {
+        const float cap = user_radii ? user_radii[q] : max_d2;
+        radii[q] = fminf(__expf(fminf(y + sp[L.margin], 80.0f)), cap);
+    }
+}
+
 // Seeded radius of each query: min(exp(prediction + margin), the caller's radius).
 __global__ void mlp_infer_kernel(const float* __restrict__ prm, uint32_t dims, const float* __restrict__ x,
                                  uint32_t count, float max_d2, const float* __restrict__ user_radii,
@@ -145,13 +231,12 @@ __global__ void mlp_infer_kernel(const float* __restrict__ prm, uint32_t dims, c
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= count) return;
     const ModelLayout L(dims);
-    float xn[kMaxDims];
-    for (uint32_t d = 0; d < dims; ++d)
-        xn[d] = (x[static_cast<size_t>(q) * dims + d] - __ldg(prm + L.mu + d)) * __ldg(prm + L.inv_sd + d);
+    float xn[kMaxDims + 2 * kFourier];
+    encode(prm, L, x + static_cast<size_t>(q) * dims, xn);
     float h1[kHidden];
     for (uint32_t i = 0; i < kHidden; ++i) {
         float a = __ldg(prm + L.b1 + i);
-        for (uint32_t d = 0; d < dims; ++d) a = fmaf(__ldg(prm + L.w1 + i * dims + d), xn[d], a);
+        for (uint32_t d = 0; d < L.feats; ++d) a = fmaf(__ldg(prm + L.w1 + i * L.feats + d), xn[d], a);
         h1[i] = fmaxf(a, 0.0f);
     }
     float y = __ldg(prm + L.b3);
@@ -169,17 +254,65 @@ __global__ void mlp_infer_kernel(const float* __restrict__ prm, uint32_t dims, c
     }
 }
 
-// Queries whose seeded radius was below the caller's and that found fewer than k points.
-__global__ void fallback_kernel(const int32_t* __restrict__ out_idx, uint32_t count, uint32_t k,
-                                const float* __restrict__ seeded, float max_d2, const float* __restrict__ user_radii,
-                                uint32_t* __restrict__ list, uint32_t* __restrict__ list_count,
-                                DevCounters* counters) {
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= count) return;
+// A query needs another search when its seeded radius was below the caller's and it found
+// fewer than k points inside it.
+__device__ __forceinline__ bool needs_retry(uint32_t q, const int32_t* out_idx, uint32_t k, const float* seeded,
+                                            float max_d2, const float* user_radii) {
     const float cap = user_radii ? user_radii[q] : max_d2;
-    if (seeded[q] < cap && out_idx[static_cast<size_t>(q) * k + (k - 1)] < 0) {
-        list[atomicAdd(list_count, 1u)] = q;
+    return seeded[q] < cap && out_idx[static_cast<size_t>(q) * k + (k - 1)] < 0;
+}
+
+constexpr uint32_t kCompactThreads = 256;
+
+__global__ void __launch_bounds__(kCompactThreads) retry_count_kernel(const uint32_t* __restrict__ order, uint32_t n,
+                                                                      const int32_t* __restrict__ out_idx, uint32_t k,
+                                                                      const float* __restrict__ seeded, float max_d2,
+                                                                      const float* __restrict__ user_radii,
+                                                                      uint32_t* __restrict__ bcnt) {
+    __shared__ uint32_t warp_tot[kCompactThreads / 32];
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    bool f = false;
+    if (p < n) f = needs_retry(order ? order[p] : p, out_idx, k, seeded, max_d2, user_radii);
+    const uint32_t c = __popc(__ballot_sync(0xFFFFFFFFu, f));
+    if ((threadIdx.x & 31) == 0) warp_tot[threadIdx.x / 32] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (uint32_t w = 0; w < kCompactThreads / 32; ++w) t += warp_tot[w];
+        bcnt[blockIdx.x] = t;
+    }
+}
+
+// Writes the retry list in the given query order (stable compaction) and grows each listed
+// query's radius: min(radius * grow, the caller's radius).
+__global__ void __launch_bounds__(kCompactThreads) retry_scatter_kernel(
+    const uint32_t* __restrict__ order, uint32_t n, const int32_t* __restrict__ out_idx, uint32_t k,
+    float* __restrict__ seeded, float max_d2, const float* __restrict__ user_radii, const uint32_t* __restrict__ bpre,
+    uint32_t nblk, float grow, uint32_t* __restrict__ list, uint32_t* __restrict__ list_count, DevCounters* counters) {
+    __shared__ uint32_t warp_tot[kCompactThreads / 32];
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x / 32;
+    uint32_t q = 0;
+    bool f = false;
+    if (p < n) {
+        q = order ? order[p] : p;
+        f = needs_retry(q, out_idx, k, seeded, max_d2, user_radii);
+    }
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, f);
+    if (lane == 0) warp_tot[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t before = bpre[blockIdx.x];
+    for (uint32_t w = 0; w < warp; ++w) before += warp_tot[w];
+    if (f) {
+        list[before + __popc(bal & ((1u << lane) - 1u))] = q;
+        const float cap = user_radii ? user_radii[q] : max_d2;
+        seeded[q] = fminf(seeded[q] * grow, cap);
         if (counters) atomicAdd(&counters->fallback, 1ull);
+    }
+    if (blockIdx.x == nblk - 1 && threadIdx.x == 0) {
+        uint32_t total = bpre[blockIdx.x];
+        for (uint32_t w = 0; w < kCompactThreads / 32; ++w) total += warp_tot[w];
+        *list_count = total;
     }
 }
 
@@ -200,12 +333,13 @@ size_t model_floats(uint32_t dims) { return ModelLayout(dims).total; }
 // summed loss (used by training and by the gradient check).
 int model_gradients(const float* d_prm, uint32_t dims, const float* d_x, const float* d_t, const uint32_t* d_rows,
                     uint32_t batch, float* d_grad, float* d_loss_rows, DevBuf& scratch, cudaStream_t s) {
-    const size_t need = carve_bytes({static_cast<size_t>(batch) * dims * 4, static_cast<size_t>(batch) * kHidden * 4,
+    const ModelLayout LL(dims);
+    const size_t need = carve_bytes({static_cast<size_t>(batch) * LL.feats * 4, static_cast<size_t>(batch) * kHidden * 4,
                                      static_cast<size_t>(batch) * kHidden * 4, static_cast<size_t>(batch) * kHidden * 4,
                                      static_cast<size_t>(batch) * kHidden * 4, static_cast<size_t>(batch) * 4});
     KNN_TRY(scratch.reserve(need));
     Carver c(scratch.ptr);
-    float* xn = c.take<float>(static_cast<size_t>(batch) * dims);
+    float* xn = c.take<float>(static_cast<size_t>(batch) * LL.feats);
     float* h1 = c.take<float>(static_cast<size_t>(batch) * kHidden);
     float* h2 = c.take<float>(static_cast<size_t>(batch) * kHidden);
     float* d1 = c.take<float>(static_cast<size_t>(batch) * kHidden);
@@ -221,18 +355,41 @@ int model_gradients(const float* d_prm, uint32_t dims, const float* d_x, const f
 
 int model_predict(const float* d_prm, uint32_t dims, const float* d_x, uint32_t count, float max_d2,
                   const float* user_radii, float* d_radii, float* d_raw, cudaStream_t s) {
+    const ModelLayout L(dims);
+    const size_t smem = static_cast<size_t>(L.total) * sizeof(float);
+    const bool aligned = (L.w2 % 4) == 0;
+#define KNN_INFER(D_)                                                                                     \
+    if (aligned && dims <= D_) {                                                                          \
+        mlp_infer_fast_kernel<D_><<<ceil_div(count, 256), 256, smem, s>>>(d_prm, dims, d_x, count, max_d2, \
+                                                                          user_radii, d_radii, d_raw);    \
+        KNN_LAUNCHED();                                                                                   \
+        return KNN_OK;                                                                                    \
+    }
+    KNN_INFER(4)
+    KNN_INFER(8)
+    KNN_INFER(16)
+#undef KNN_INFER
     mlp_infer_kernel<<<ceil_div(count, 128), 128, 0, s>>>(d_prm, dims, d_x, count, max_d2, user_radii, d_radii,
                                                           d_raw);
     KNN_LAUNCHED();
     return KNN_OK;
 }
 
-int model_fallbacks(const int32_t* out_idx, uint32_t count, uint32_t k, const float* seeded, float max_d2,
-                    const float* user_radii, uint32_t* list, uint32_t* list_count, DevCounters* counters,
-                    cudaStream_t s) {
-    KNN_TRY_CUDA(cudaMemsetAsync(list_count, 0, sizeof(uint32_t), s));
-    fallback_kernel<<<ceil_div(count, 256), 256, 0, s>>>(out_idx, count, k, seeded, max_d2, user_radii, list,
-                                                         list_count, counters);
+size_t retry_scratch_bytes(uint32_t count) {
+    return 2 * static_cast<size_t>(ceil_div(count, kCompactThreads)) * sizeof(uint32_t) + 512;
+}
+
+int model_retry_list(const uint32_t* order, const int32_t* out_idx, uint32_t count, uint32_t k, float* seeded,
+                     float max_d2, const float* user_radii, float grow, uint32_t* list, uint32_t* list_count,
+                     void* scratch, DevCounters* counters, cudaStream_t s) {
+    const uint32_t nblk = ceil_div(count, kCompactThreads);
+    uint32_t* bcnt = static_cast<uint32_t*>(scratch);
+    uint32_t* bpre = bcnt + nblk;
+    retry_count_kernel<<<nblk, kCompactThreads, 0, s>>>(order, count, out_idx, k, seeded, max_d2, user_radii, bcnt);
+    KNN_LAUNCHED();
+    KNN_TRY(scan_rows_exclusive(bcnt, bpre, 1, nblk, s));
+    retry_scatter_kernel<<<nblk, kCompactThreads, 0, s>>>(order, count, out_idx, k, seeded, max_d2, user_radii, bpre,
+                                                          nblk, grow, list, list_count, counters);
     KNN_LAUNCHED();
     return KNN_OK;
 }
@@ -279,23 +436,21 @@ int model_train(knn_index* ix, const float* d_samples, uint32_t count, uint32_t 
     KNN_TRY_CUDA(cudaStreamSynchronize(s));
     std::vector<float> hp(L.total, 0.0f);
     for (uint32_t d = 0; d < dims; ++d) {
-        double mean = 0, sq = 0;
-        for (uint32_t i = 0; i < count; ++i) mean += hx[static_cast<size_t>(i) * dims + d];
-        mean /= count;
+        float lo = INFINITY, hi = -INFINITY;
         for (uint32_t i = 0; i < count; ++i) {
-            const double t = hx[static_cast<size_t>(i) * dims + d] - mean;
-            sq += t * t;
+            lo = std::min(lo, hx[static_cast<size_t>(i) * dims + d]);
+            hi = std::max(hi, hx[static_cast<size_t>(i) * dims + d]);
         }
-        const double sd = std::sqrt(sq / std::max(1u, count)) + 1e-12;
-        hp[L.mu + d] = static_cast<float>(mean);
-        hp[L.inv_sd + d] = static_cast<float>(1.0 / sd);
+        hp[L.lo + d] = lo;
+        hp[L.inv_range + d] = hi > lo ? 1.0f / (hi - lo) : 1.0f;
     }
     double tmean = 0;
     for (float t : ht) tmean += t;
     tmean /= std::max(1u, count);
     std::mt19937 gen(o.seed);
     std::normal_distribution<float> nd(0.0f, 1.0f);
-    for (uint32_t i = 0; i < kHidden * dims; ++i) hp[L.w1 + i] = nd(gen) * std::sqrt(2.0f / dims);
+    for (uint32_t i = 0; i < dims * kFourier; ++i) hp[L.proj + i] = nd(gen) * kFourierScale;
+    for (uint32_t i = 0; i < kHidden * L.feats; ++i) hp[L.w1 + i] = nd(gen) * std::sqrt(2.0f / L.feats);
     for (uint32_t i = 0; i < kHidden * kHidden; ++i) hp[L.w2 + i] = nd(gen) * std::sqrt(2.0f / kHidden);
     for (uint32_t i = 0; i < kHidden; ++i) hp[L.w3 + i] = nd(gen) * std::sqrt(1.0f / kHidden);
     hp[L.b3] = static_cast<float>(tmean);
@@ -318,7 +473,7 @@ int model_train(knn_index* ix, const float* d_samples, uint32_t count, uint32_t 
         KNN_TRY(model_gradients(prm, dims, d_samples, target, rows + offset, batch, grad, loss_rows, scratch, s));
         c1 *= b1;
         c2 *= b2;
-        const float lr = o.lr * (step < o.steps / 2 ? 1.0f : (step < 3 * o.steps / 4 ? 0.3f : 0.1f));
+        const float lr = o.lr * 0.5f * (1.0f + std::cos(3.14159265f * static_cast<float>(step) / o.steps));
         adam_kernel<<<ceil_div(L.trainable, 256), 256, 0, s>>>(prm, grad, m, v, L.trainable, lr, b1, b2, 1e-8f,
                                                               1.0f - c1, 1.0f - c2);
         KNN_LAUNCHED();

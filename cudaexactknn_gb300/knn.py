@@ -123,9 +123,9 @@ class _Index:
 
     def batch_knn(self, query: Query, k: int | None = None, block_size: int = 0, heap: bool = False,
                   shmem_tracking: bool = False, shmem_stack: bool = False, flags: int = 0,
-                  leaf_scan: int = 0, sync: bool = True, stream=None):
+                  leaf_scan: int = 0, traversal: int = 0, tc_cap: int = 0, sync: bool = True, stream=None):
         """batchKnn<K,BLOCK_SIZE,USE_HEAP_TRACKING,USE_TRACKING_SHMEM,USE_STACK_SHMEM>(query)."""
-        o = _lib.opts(block_size, heap, shmem_tracking, shmem_stack, flags, leaf_scan)
+        o = _lib.opts(block_size, heap, shmem_tracking, shmem_stack, flags, leaf_scan, traversal, tc_cap)
         return self._query(query, k, o, sync, stream)
 
     def batch_knn_radii(self, query: Query, radii: torch.Tensor, k: int | None = None, sync: bool = True,
@@ -142,7 +142,8 @@ class _Index:
         return self.batch_knn(q, k, **kw)
 
     def knn_host(self, queries, k: int, max_distance2: float = math.inf, out_idx=None, out_dist=None,
-                 block_size=0, heap=False, shmem_tracking=False, shmem_stack=False, flags=0, stream=None):
+                 block_size=0, heap=False, shmem_tracking=False, shmem_stack=False, flags=0, leaf_scan=0,
+                 traversal=0, stream=None):
         """End-to-end query on host buffers (numpy or CPU tensors; pinned memory is fastest)."""
         qt = torch.as_tensor(queries)
         if qt.dtype != torch.float32 or not qt.is_contiguous() or qt.is_cuda:
@@ -152,7 +153,7 @@ class _Index:
             out_idx = torch.empty((count, k), dtype=torch.int32, pin_memory=qt.is_pinned())
         if out_dist is None:
             out_dist = torch.empty((count, k), dtype=torch.float32, pin_memory=qt.is_pinned())
-        o = _lib.opts(block_size, heap, shmem_tracking, shmem_stack, flags)
+        o = _lib.opts(block_size, heap, shmem_tracking, shmem_stack, flags, leaf_scan, traversal)
         st = _lib.load().knn_query_host(self._h, qt.data_ptr(), count, float(max_distance2), k,
                                         out_idx.data_ptr(), out_dist.data_ptr(), ctypes.byref(o),
                                         _stream_handle(stream))
@@ -267,7 +268,7 @@ def radius_model_gradients(params, dims: int, x, targets):
     xb = np.ascontiguousarray(x, np.float32)
     tb = np.ascontiguousarray(targets, np.float32)
     n = lib.knn_radius_model_size(dims)
-    trainable = n - 2 * dims - 1
+    trainable = n - dims * 32 - 2 * dims - 1
     grad = np.empty(trainable, np.float32)
     loss = ctypes.c_float()
     _lib.check(lib.knn_radius_model_gradients(p.ctypes.data, dims, xb.ctypes.data, tb.ctypes.data, len(tb),

@@ -95,7 +95,10 @@ typedef struct knn_query_opts {
     uint32_t flags;
     uint32_t leaf_scan;     /* trees: scan whole subtrees of at most this many points as one
                                leaf (0 = the tree's own leaves) */
-    uint32_t reserved[2];
+    uint32_t traversal;     /* trees: 0 = one depth-first search per thread (the reference's
+                               scheme), 1 = warp-coherent search (a warp's queries walk together) */
+    uint32_t reserved;      /* KNN_QF_BF16_FILTER: candidates kept per query (0 = 4096); for
+                               knn_tuned_plan, the number of candidate plans timed */
 } knn_query_opts;
 
 /* Per-query statistics written by knn_query_stats (summed over the batch). */
@@ -123,7 +126,7 @@ typedef struct knn_index_info {
 
 /* Learned-radius training options; zeros select the defaults in brackets. */
 typedef struct knn_train_opts {
-    uint32_t steps;   /* Adam steps [1500] */
+    uint32_t steps;   /* Adam steps, cosine-decayed learning rate [3000] */
     uint32_t batch;   /* samples per step [1024] */
     float lr;         /* learning rate [3e-3] */
     float coverage;   /* fraction of training queries whose k-th distance must fall inside the
@@ -198,10 +201,15 @@ KNN_API int knn_radius_model_gradients(const float* h_params, uint32_t dims, con
 KNN_API int knn_last_query_timing(knn_index* index, float* total_ms, float* kernel_ms);
 
 /* The plan KNN_QF_AUTOTUNE chose for this index and k (block size, tracking, storage, leaf
- * bucket), with the tuning sample's time in *ms and the number of candidates timed in
- * out->reserved[0].  Autotuning runs on the first KNN_QF_AUTOTUNE query per k class. */
+ * bucket, traversal), with the tuning sample's time in *ms and the number of candidates timed
+ * in out->reserved.  Autotuning runs on the first KNN_QF_AUTOTUNE query per k class. */
 KNN_API int knn_tuned_plan(const knn_index* index, uint32_t k, uint32_t learned_radius, knn_query_opts* out,
                            float* ms);
+
+/* Runs one 128 x 256 tile with K = dims through the tensor-core path (tcgen05.mma, BF16 in, FP32
+ * accumulate) on fixed data and compares it with exact products of the BF16-rounded inputs:
+ * worst relative error and the count of entries beyond the bound the filter assumes. */
+KNN_API int knn_tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* mismatches);
 
 /* Number of kernels this library has launched since it was loaded (all indexes, all threads). */
 KNN_API uint64_t knn_launch_count(void);

@@ -91,10 +91,11 @@ def test_variants(structure, heap, shmem_tracking, shmem_stack):
     qs = W.uniform(rng, 5000, 5)
     want = _oracle(pts, qs, 12)
     ix = gu.make_index(structure, pts, 2)
-    for block in (32, 128, 256):
-        got = gu.run(ix, qs, 12, block_size=block, heap=heap, shmem_tracking=shmem_tracking,
-                     shmem_stack=shmem_stack)
-        gu.assert_rows_equal(*got, *want, what=f"{structure} block={block}")
+    for traversal in ((0, 1) if structure != "bf" else (0,)):
+        for block in (32, 128, 256):
+            got = gu.run(ix, qs, 12, block_size=block, heap=heap, shmem_tracking=shmem_tracking,
+                         shmem_stack=shmem_stack, traversal=traversal)
+            gu.assert_rows_equal(*got, *want, what=f"{structure} block={block} traversal={traversal}")
 
 
 # ---- dimensions and k across every compiled class --------------------------------------------
@@ -110,6 +111,8 @@ def test_dims(structure, dims):
     want = _oracle(pts, qs, k)
     ix = gu.make_index(structure, pts, 1)
     gu.assert_rows_equal(*gu.run(ix, qs, k), *want, what=f"{structure} D={dims}")
+    if structure != "bf":
+        gu.assert_rows_equal(*gu.run(ix, qs, k, traversal=1), *want, what=f"{structure} D={dims} warp")
 
 
 @pytest.mark.parametrize("k", [1, 2, 7, 8, 9, 16, 17, 31, 32, 33, 64, 65, 100, 128])
@@ -137,7 +140,9 @@ def test_small_and_ragged_n(structure, n):
         want = _oracle(pts, qs, k, r2)
         for skips in (0, 1, 3, 40):
             ix = gu.make_index(structure, pts, skips)
-            gu.assert_rows_equal(*gu.run(ix, qs, k, r2), *want, what=f"{structure} n={n} skips={skips} r2={r2}")
+            for traversal in (0, 1):
+                gu.assert_rows_equal(*gu.run(ix, qs, k, r2, traversal=traversal), *want,
+                                     what=f"{structure} n={n} skips={skips} r2={r2} traversal={traversal}")
             ix.close()
 
 
@@ -162,7 +167,9 @@ def test_duplicates_and_exact_ties(structure):
         want = _oracle(grid, qs, k)
         for skips in (0, 2):
             ix = gu.make_index(structure, grid, skips)
-            gu.assert_rows_equal(*gu.run(ix, qs, k), *want, what=f"{structure} ties k={k} skips={skips}")
+            for traversal in (0, 1):
+                gu.assert_rows_equal(*gu.run(ix, qs, k, traversal=traversal), *want,
+                                     what=f"{structure} ties k={k} skips={skips} traversal={traversal}")
 
 
 @pytest.mark.parametrize("structure", ["bf", "kd", "ball"])
@@ -249,7 +256,7 @@ def test_autotune_is_exact_and_reports_its_plan(structure, dims, k):
     ms = ctypes.c_float()
     _lib.check(_lib.load().knn_tuned_plan(ix.handle, k, 0, ctypes.byref(o), ctypes.byref(ms)))
     assert o.block_size in (32, 64, 128, 256) and ms.value > 0
-    assert o.reserved[0] >= (7 if structure == "bf" else 10)
+    assert o.reserved >= (7 if structure == "bf" else 10)
     # The tuned plan is reused on later calls and still exact.
     gu.assert_rows_equal(*gu.run(ix, qs, k, flags=_lib.QF_AUTOTUNE), *want, what=f"{structure} autotune again")
 
@@ -262,4 +269,6 @@ def test_leaf_bucket_scan(structure, leaf_scan):
     qs = W.uniform(rng, 700, 4)
     want = _oracle(pts, qs, 9)
     ix = gu.make_index(structure, pts, 1)
-    gu.assert_rows_equal(*gu.run(ix, qs, 9, leaf_scan=leaf_scan), *want, what=f"{structure} leaf_scan={leaf_scan}")
+    for traversal in (0, 1):
+        gu.assert_rows_equal(*gu.run(ix, qs, 9, leaf_scan=leaf_scan, traversal=traversal), *want,
+                             what=f"{structure} leaf_scan={leaf_scan} traversal={traversal}")

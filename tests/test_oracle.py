@@ -117,3 +117,24 @@ def test_oracle_fma_mode_is_a_single_rounding_per_step(dims):
         want = _fma_dist2_exact(a, b)
         got = np.float32(oracle.dist2(a, b, fma=True))
         assert got.view(np.uint32) == want.view(np.uint32)
+
+
+def test_radius_model_reference_gradient_is_consistent():
+    """The float64 model restatement (the checker of the GPU kernels) against central differences."""
+    import radius_model_ref as ref
+    rng = np.random.default_rng(0)
+    d = 3
+    e = d + 64
+    n = 64 * e + 64 + 64 * 64 + 64 + 64 + 1
+    p = np.zeros(n + 32 * d + 2 * d + 1)
+    p[:n] = rng.standard_normal(n) * 0.2
+    p[n:n + 32 * d] = rng.standard_normal(32 * d) * 4
+    p[n + 33 * d:n + 34 * d] = 0.5
+    x = rng.standard_normal((50, d))
+    t = rng.standard_normal(50)
+    _, g = ref.loss_and_grad(p, d, x, t)
+    for i in rng.choice(len(g), size=30, replace=False):
+        h = np.zeros_like(p)
+        h[i] = 1e-5
+        num = (ref.loss_and_grad(p + h, d, x, t)[0] - ref.loss_and_grad(p - h, d, x, t)[0]) / 2e-5
+        assert abs(g[i] - num) <= 1e-6 * max(1.0, abs(num))

@@ -13,11 +13,13 @@ gu = pytest.importorskip("gpu_util")
 
 
 def _random_params(d, rng):
-    n = 64 * d + 64 + 64 * 64 + 64 + 64 + 1
-    p = np.zeros(n + 2 * d + 1, np.float32)
-    p[:n] = rng.standard_normal(n).astype(np.float32) * 0.3
-    p[n:n + d] = rng.standard_normal(d) * 0.1          # mu
-    p[n + d:n + 2 * d] = 1.0 + rng.random(d)            # inv_sd
+    e = d + 64
+    n = 64 * e + 64 + 64 * 64 + 64 + 64 + 1
+    p = np.zeros(n + 32 * d + 2 * d + 1, np.float32)
+    p[:n] = rng.standard_normal(n).astype(np.float32) * 0.2
+    p[n:n + 32 * d] = rng.standard_normal(32 * d) * 4.0            # projection B
+    p[n + 32 * d:n + 33 * d] = -1.0 + 0.1 * rng.standard_normal(d)  # lo
+    p[n + 33 * d:n + 34 * d] = 0.3 + 0.1 * rng.random(d)            # inv_range
     return p
 
 
@@ -32,7 +34,7 @@ def test_gradients_match_float64_oracle(d):
     want_loss, want_grad = ref.loss_and_grad(p, d, x, t)
     assert abs(loss - want_loss) <= 1e-4 * max(1.0, abs(want_loss))
     scale = np.abs(want_grad).max()
-    np.testing.assert_allclose(grad, want_grad, rtol=2e-3, atol=2e-5 * scale)
+    np.testing.assert_allclose(grad, want_grad, rtol=2e-3, atol=1e-4 * scale)
 
 
 def test_gradients_match_finite_differences():
@@ -43,11 +45,15 @@ def test_gradients_match_finite_differences():
     x = rng.standard_normal((64, d))
     t = rng.standard_normal(64)
     _, g = knn.radius_model_gradients(p, d, x, t)
+    # Central differences of the float64 loss agree with the GPU gradient; the reference's own
+    # analytic gradient agrees with both.
+    _, g64 = ref.loss_and_grad(p, d, x, t)
     for i in rng.choice(len(g), size=25, replace=False):
         e = np.zeros_like(p)
-        e[i] = 1e-3
-        num = (ref.loss_and_grad(p + e, d, x, t)[0] - ref.loss_and_grad(p - e, d, x, t)[0]) / 2e-3
-        assert abs(g[i] - num) <= 2e-3 * max(1.0, abs(num)), i
+        e[i] = 1e-4
+        num = (ref.loss_and_grad(p + e, d, x, t)[0] - ref.loss_and_grad(p - e, d, x, t)[0]) / 2e-4
+        assert abs(g64[i] - num) <= 1e-5 * max(1.0, abs(num)), i
+        assert abs(g[i] - num) <= 2e-3 * max(1.0, abs(num)) + 1e-4 * np.abs(g64).max(), i
 
 
 @pytest.mark.parametrize("structure,skips,d,k", [("kd", 0, 3, 16), ("ball", 1, 16, 32), ("bf", 0, 8, 10)])

@@ -1,0 +1,87 @@
+"""Brute force through the BF16 tensor-core filter (tcgen05) with exact FP32 rescoring.
+
+The filter is only a filter: every returned row must equal the plain brute force's exactly
+(same keys: indices, tie order and distance bits), whatever the data, k or radius."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from cudaexactknn_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+gu = pytest.importorskip("gpu_util")
+
+
+def _flags():
+    from cudaexactknn_gb300 import _lib
+    return _lib.QF_BF16_FILTER
+
+
+@pytest.mark.parametrize("dims", [16, 40, 64, 100, 128])
+def test_tensor_core_selftest(dims):
+    """tcgen05.mma over one 128x256 tile matches exact products of the BF16 inputs."""
+    from cudaexactknn_gb300 import _lib
+    err = ctypes.c_float()
+    bad = ctypes.c_uint32()
+    _lib.check(_lib.load().knn_tc_selftest(dims, ctypes.byref(err), ctypes.byref(bad)))
+    assert bad.value == 0, (bad.value, err.value)
+    assert err.value <= dims * 2.0 ** -20
+
+
+@pytest.mark.parametrize("dims", [16, 17, 32, 64, 100, 128])
+@pytest.mark.parametrize("k", [1, 10, 100])
+def test_filter_exact(dims, k):
+    rng = np.random.default_rng(dims * 1000 + k)
+    pts, centres = W.gauss_mix(rng, 6000, dims, 24, 0.3)
+    qs, _ = W.gauss_mix(rng, 300, dims, 24, 0.3, centres)
+    ix = gu.make_index("bf", pts)
+    want = oracle.bf_knn(pts, qs, k, fma=True, threads=8)
+    gu.assert_rows_equal(*gu.run(ix, qs, k, flags=_flags()), *want, what=f"bf16 filter D={dims} k={k}")
+
+
+@pytest.mark.parametrize("n,nq", [(1, 5), (255, 129), (257, 127), (1025, 1), (3000, 1000)])
+def test_filter_ragged_sizes(n, nq):
+    rng = np.random.default_rng(n)
+    pts = W.uniform(rng, n, 24)
+    qs = W.uniform(rng, nq, 24)
+    ix = gu.make_index("bf", pts)
+    for r2 in (float("inf"), 2.0):
+        want = oracle.bf_knn(pts, qs, 16, r2, fma=True, threads=8)
+        gu.assert_rows_equal(*gu.run(ix, qs, 16, r2, flags=_flags()), *want, what=f"n={n} nq={nq} r2={r2}")
+
+
+def test_filter_ties_and_duplicates():
+    rng = np.random.default_rng(3)
+    grid = (rng.integers(0, 3, size=(4000, 16)) / 2.0).astype(np.float32)
+    qs = np.concatenate([grid[:100], (rng.integers(0, 3, size=(100, 16)) / 2.0).astype(np.float32)])
+    ix = gu.make_index("bf", grid)
+    for k in (1, 32, 128):
+        want = oracle.bf_knn(grid, qs, k, fma=True, threads=8)
+        gu.assert_rows_equal(*gu.run(ix, qs, k, flags=_flags()), *want, what=f"grid ties k={k}")
+
+
+def test_candidate_overflow_falls_back_exactly():
+    rng = np.random.default_rng(4)
+    pts = W.uniform(rng, 5000, 32)
+    qs = W.uniform(rng, 700, 32)
+    ix = gu.make_index("bf", pts)
+    want = oracle.bf_knn(pts, qs, 20, fma=True, threads=8)
+    # A candidate capacity below k forces every query through the plain path.
+    gu.assert_rows_equal(*gu.run(ix, qs, 20, flags=_flags(), tc_cap=8), *want, what="cap 8")
+    gu.assert_rows_equal(*gu.run(ix, qs, 20, flags=_flags(), tc_cap=64), *want, what="cap 64")
+
+
+def test_filter_with_learned_radius():
+    from cudaexactknn_gb300 import _lib
+    rng = np.random.default_rng(6)
+    pts, centres = W.gauss_mix(rng, 20000, 64, 32, 0.3)
+    qs, _ = W.gauss_mix(rng, 1500, 64, 32, 0.3, centres)
+    train, _ = W.gauss_mix(rng, 4096, 64, 32, 0.3, centres)
+    ix = gu.make_index("bf", pts)
+    ix.train_radius_model(gu.to_dev(train), 50, steps=300)
+    want = oracle.bf_knn(pts, qs, 50, fma=True, threads=8)
+    got = gu.run(ix, qs, 50, flags=_flags() | _lib.QF_LEARNED_RADIUS)
+    gu.assert_rows_equal(*got, *want, what="bf16 filter + learned radius")
