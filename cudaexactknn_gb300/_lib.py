@@ -98,6 +98,7 @@ _SIGNATURES = {
     "knn_radius_model_gradients": [_vp, _u32, _vp, _vp, _u32, _vp, _vp],
     "knn_last_query_timing": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
     "knn_launch_count": [],
+    "knn_bf_query_noalloc": [_vp, _u32, _u32, _vp, _u32, _f, _u32, _vp, _vp, _vp],
     "knn_tc_selftest": [_u32, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint32)],
     "knn_tuned_plan": [_vp, _u32, _u32, ctypes.POINTER(QueryOpts), ctypes.POINTER(ctypes.c_float)],
     "knn_status_string": [ctypes.c_int],

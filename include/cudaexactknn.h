@@ -206,6 +206,19 @@ KNN_API int knn_last_query_timing(knn_index* index, float* total_ms, float* kern
 KNN_API int knn_tuned_plan(const knn_index* index, uint32_t k, uint32_t learned_radius, knn_query_opts* out,
                            float* ms);
 
+/* Brute-force query that allocates no device memory.  No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc (inside a stream capture, under an allocator that
+ * forbids side allocations, in a loop that must not touch the allocator) and so cannot create an
+ * index either.  Searches the caller's device points [n][dims] directly; its only scratch is a
+ * 16 MiB array compiled into the library (held on every GPU that loads the library, until exit).
+ * Limit: count * k <= 1,048,576, else KNN_ERR_UNSUPPORTED.  All calls on a device share that
+ * array, so calls that overlap on the GPU race; the first call on each device looks up the
+ * array's address and should come before any stream capture.  Same results as knn_query on a
+ * brute-force index of the same points. */
+KNN_API int knn_bf_query_noalloc(const float* d_points, uint32_t n, uint32_t dims, const float* d_queries,
+                                 uint32_t count, float max_distance2, uint32_t k, int32_t* d_indexes,
+                                 float* d_distances, void* stream);
+
 /* Runs one 128 x 256 tile with K = dims through the tensor-core path (tcgen05.mma, BF16 in, FP32
  * accumulate) on fixed data and compares it with exact products of the BF16-rounded inputs:
  * worst relative error and the count of entries beyond the bound the filter assumes. */
