@@ -70,6 +70,14 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def bf16_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
 def profile_traffic(kernel: str, workload: str):
     """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if one exists."""
     path = os.path.join(ROOT, "profiles", f"ncu_{kernel}_{workload}.txt")
@@ -351,7 +359,8 @@ def main():
     tuned_ms = ctypes.c_float()
     learned = bool(chosen_kw.get("flags", 0) & _lib.QF_LEARNED_RADIUS)
     _lib.check(lib.knn_tuned_plan(index.handle, k, int(learned), ctypes.byref(tuned), ctypes.byref(tuned_ms)))
-    tuned_plan = dict(block_size=tuned.block_size, heap=bool(tuned.heap_tracking),
+    tuned_plan = dict(bf16_filter=bool(tuned.flags & _lib.QF_BF16_FILTER), block_size=tuned.block_size,
+                      heap=bool(tuned.heap_tracking),
                       shmem_tracking=bool(tuned.shmem_tracking), shmem_stack=bool(tuned.shmem_stack),
                       leaf_scan=tuned.leaf_scan, traversal="warp" if tuned.traversal else "thread",
                       candidates_timed=tuned.reserved)
@@ -383,9 +392,18 @@ def main():
     e2e_qps = world * count * args.steps / e2e_s
     e2e_exact = float((oracle.row_keys(h_i.numpy()[sample], h_d.numpy()[sample]) == want).all(axis=1).mean())
 
-    peak, peak_kind = peaks()
     kernel_name = {"kd": "kd_knn_kernel", "ball": "ball_knn_kernel", "bf": "bf_knn_kernel"}[w.structure]
-    achieved = alg_bytes / (chosen_kern_ms / 1e3) / 1e9
+    if tuned_plan.get("bf16_filter"):
+        # Brute force through the tensor cores: 2 N D flops per query in the BF16 GEMM.
+        kernel_name = "tc_filter_kernel"
+        peak, peak_kind = bf16_peak()
+        flops = 2.0 * w.points.shape[0] * w.dims * count
+        achieved = flops / (chosen_kern_ms / 1e3) / 1e12
+        roof_bound, roof_unit = "tensor", "TFLOP/s"
+    else:
+        peak, peak_kind = peaks()
+        achieved = alg_bytes / (chosen_kern_ms / 1e3) / 1e9
+        roof_bound, roof_unit = "hbm", "GB/s"
     traffic = profile_traffic(kernel_name, args.workload)
 
     line = {
@@ -398,7 +416,7 @@ def main():
         "exact_match": {"chosen": exact["chosen"], "plain": exact["plain"], "e2e": e2e_exact,
                         "sample_queries": int(len(sample))},
         "plain": {"value": plain_qps, "ms_per_step": plain_ms / args.steps, "plan": plain_kw,
-                  "kernel_ms": plain_kern_ms, "roofline_frac": alg_bytes / (plain_kern_ms / 1e3) / 1e9 / peaks()[0]},
+                  "kernel_ms": plain_kern_ms},
         "chosen": {"form": "autotune + learned radius" if learned else "autotune", "plan": tuned_plan,
                    "kernel_ms": chosen_kern_ms, "speedup_vs_plain": value / plain_qps,
                    "fallback_queries": int(chosen_counters.fallback_queries),
@@ -413,9 +431,9 @@ def main():
                 "h2d_bytes_per_step": int(w.queries.nbytes),
                 "d2h_bytes_per_step": int(count * k * 8)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": roof_bound, "achieved": achieved, "peak": peak, "unit": roof_unit,
                      "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "peak_source": f"{peak_kind} " + ("bf16_tflops" if roof_bound == "tensor" else "hbm_gbs"),
                      "kernel": kernel_name, "algorithmic_bytes_per_launch": int(alg_bytes),
                      "compulsory_bytes_per_launch": int(floor_bytes),
                      "visits": {"nodes": int(counters.nodes_visited), "leaves": int(counters.leaves_visited),

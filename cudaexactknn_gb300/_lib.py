@@ -66,6 +66,12 @@ class TrainReport(ctypes.Structure):
                 ("steps", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
+class BatchItem(ctypes.Structure):
+    _fields_ = [("index", ctypes.c_void_p), ("d_queries", ctypes.c_void_p), ("count", ctypes.c_uint32),
+                ("max_distance2", ctypes.c_float), ("k", ctypes.c_uint32), ("d_indexes", ctypes.c_void_p),
+                ("d_distances", ctypes.c_void_p)]
+
+
 class KnnError(RuntimeError):
     """A non-zero knn_status; ``.status`` holds the code (the reference throws CudaException)."""
 
@@ -98,6 +104,10 @@ _SIGNATURES = {
     "knn_radius_model_gradients": [_vp, _u32, _vp, _vp, _u32, _vp, _vp],
     "knn_last_query_timing": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
     "knn_launch_count": [],
+    "knn_batch_create": [ctypes.POINTER(BatchItem), _u32, _u32, _vp, _pp],
+    "knn_batch_run": [_vp, _vp],
+    "knn_batch_info": [_vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)],
+    "knn_batch_destroy": [_vp],
     "knn_bf_query_noalloc": [_vp, _u32, _u32, _vp, _u32, _f, _u32, _vp, _vp, _vp],
     "knn_tc_selftest": [_u32, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint32)],
     "knn_tuned_plan": [_vp, _u32, _u32, ctypes.POINTER(QueryOpts), ctypes.POINTER(ctypes.c_float)],

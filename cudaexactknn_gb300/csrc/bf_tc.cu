@@ -59,7 +59,9 @@ struct TcParams {
     uint32_t n, nq, ptiles;
     float c1, c2, g;
     float max_d2;
-    const float* radii;   // per-query radius or null
+    const float* radii;   // per-query radius or null (indexed by query)
+    const uint32_t* order;       // row -> query, or null
+    const uint32_t* live_count;  // rows in use (device), or null for nq
     uint32_t k;
     uint32_t cap;
     uint32_t* cand;       // [nq][cap]
@@ -103,7 +105,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     uint8_t* sA = smem;
     uint8_t* sB0 = sA + H * kTileM * 128u;
     uint8_t* sB1 = sB0 + H * kTileN * 128u;
-    float* heap_base = reinterpret_cast<float*>(sB1 + H * kTileN * 128u);
+    float2* sN = reinterpret_cast<float2*>(sB1 + H * kTileN * 128u);  // [2][kTileN] point norms
+    float* heap_base = reinterpret_cast<float*>(sN + 2 * kTileN);
     uint64_t* bars = reinterpret_cast<uint64_t*>(heap_base + static_cast<size_t>(p.k) * kTileM);
     uint64_t* full = bars;         // [2] B stage loaded
     uint64_t* empty = bars + 2;    // [2] B stage consumed by the MMAs
@@ -114,6 +117,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint32_t live_rows = p.live_count ? *p.live_count : p.nq;
+    if (blockIdx.x * kTileM >= live_rows) return;  // whole block idle: leave before any allocation
     if (threadIdx.x == 0) {
         for (int i = 0; i < 2; ++i) {
             mbar_init(full + i, 1);
@@ -138,14 +143,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
             mbar_expect_tx(a_full, a_bytes(H));
             bulk_copy_g2s(sA, p.qimg + static_cast<size_t>(blockIdx.x) * a_bytes(H), a_bytes(H), a_full);
             uint32_t issued = 0;
+            constexpr uint32_t kNormBytes = kTileN * sizeof(float2);
             for (uint32_t t = 0; t < ptiles; ++t) {
                 const uint32_t s = t & 1;
-                if (t >= 2 && !mbar_wait(empty + s, ((t >> 1) - 1) & 1, abort)) {
+                // Stage s is free once the MMAs of tile t-2 are done (operands) and the epilogue
+                // has drained tile t-2 (its norms).
+                if (t >= 2 && (!mbar_wait(empty + s, ((t >> 1) - 1) & 1, abort) ||
+                               !mbar_wait(acc_empty + s, ((t >> 1) - 1) & 1, abort))) {
                     *abort = 1;
                     break;
                 }
-                mbar_expect_tx(full + s, b_bytes(H));
+                mbar_expect_tx(full + s, b_bytes(H) + kNormBytes);
                 bulk_copy_g2s(s ? sB1 : sB0, p.pimg + static_cast<size_t>(t) * b_bytes(H), b_bytes(H), full + s);
+                bulk_copy_g2s(sN + s * kTileN, p.pnorm + static_cast<size_t>(t) * kTileN, kNormBytes, full + s);
                 ++issued;
             }
             if (*abort) {
@@ -190,10 +200,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         // Epilogue: thread = query row.  TMEM lanes 32*(warp%4) .. +31 belong to this warp.
         const uint32_t quarter = warp & 3;
         const uint32_t row = quarter * 32 + lane;
-        const uint32_t q = blockIdx.x * kTileM + row;
-        const bool live = q < p.nq;
+        const uint32_t q = blockIdx.x * kTileM + row;  // row of the batch (position in the list)
+        const bool live = q < live_rows;
+        const uint32_t qi = live ? (p.order ? p.order[q] : q) : 0u;
         const float2 qn = live ? p.qnorm[q] : make_float2(0.0f, 0.0f);
-        const float seed = live ? (p.radii ? fminf(p.radii[q], p.max_d2) : p.max_d2) : 0.0f;
+        const float seed = live ? (p.radii ? fminf(p.radii[qi], p.max_d2) : p.max_d2) : 0.0f;
         BoundHeap heap{heap_base + row, p.k};
         for (uint32_t i = 0; i < p.k; ++i) heap.at(i) = seed;
         float T = seed;
@@ -215,13 +226,15 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         for (uint32_t t = 0; t < ptiles; ++t) {
             const uint32_t b = t & 1;
             // The TMEM loads below are warp-collective: the whole warp proceeds or leaves.
-            const bool got = mbar_wait(acc_full + b, (t >> 1) & 1, abort);
+            // acc_full: the MMAs are done; full: this tile's norms landed in shared memory
+            // (already complete, waited on to observe the copy's writes).
+            const bool got = mbar_wait(acc_full + b, (t >> 1) & 1, abort) && mbar_wait(full + b, (t >> 1) & 1, abort);
             if (!__all_sync(0xFFFFFFFFu, got)) {
                 ok = false;
                 break;
             }
             tc_fence_after();
-            const float2* pn = p.pnorm + static_cast<size_t>(t) * kTileN;
+            const float2* pn = sN + b * kTileN;
             const uint32_t base = t * kTileN;
 #pragma unroll 1
             for (uint32_t c = 0; c < kTileN / 32; ++c) {
@@ -230,7 +243,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
 #pragma unroll
                 for (uint32_t i = 0; i < 32; ++i) {
                     const uint32_t jl = c * 32 + i;
-                    const float2 pp = __ldg(pn + jl);
+                    const float2 pp = pn[jl];
                     const float theta = __fmaf_rd(alpha, pp.x, __fmaf_rd(-beta, pp.y, gam));
                     if (live && v[i] >= theta && base + jl < p.n) {
                         if (count < p.cap) my_cand[count] = base + jl;
@@ -270,27 +283,30 @@ __global__ void __launch_bounds__(128) tc_rescore_kernel(const float* __restrict
                                                          uint32_t dims, uint32_t nq, const uint32_t* __restrict__ cand,
                                                          const uint32_t* __restrict__ cand_count, uint32_t cap, uint32_t k,
                                                          float max_d2, const float* __restrict__ radii,
+                                                         const uint32_t* __restrict__ order,
+                                                         const uint32_t* __restrict__ live_count,
                                                          int32_t* __restrict__ out_idx, float* __restrict__ out_dist,
                                                          uint32_t* __restrict__ retry, uint32_t* __restrict__ retry_count) {
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nq) return;
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;  // row of the batch
+    if (q >= (live_count ? *live_count : nq)) return;
+    const uint32_t qi = order ? order[q] : q;
     const uint32_t cnt = cand_count[q];
     if (cnt > cap) {
-        retry[atomicAdd(retry_count, 1u)] = q;
+        retry[atomicAdd(retry_count, 1u)] = qi;
         return;
     }
     float qv[PS];
 #pragma unroll
-    for (int d = 0; d < PS; ++d) qv[d] = static_cast<uint32_t>(d) < dims ? queries[static_cast<size_t>(q) * dims + d] : 0.0f;
+    for (int d = 0; d < PS; ++d) qv[d] = static_cast<uint32_t>(d) < dims ? queries[static_cast<size_t>(qi) * dims + d] : 0.0f;
     Tracker<KMAX, false, false> tr;
-    tr.init(k, radii ? fminf(radii[q], max_d2) : max_d2, nullptr, 0);
+    tr.init(k, radii ? fminf(radii[qi], max_d2) : max_d2, nullptr, 0);
     const uint32_t* c = cand + static_cast<size_t>(q) * cap;
     for (uint32_t i = 0; i < cnt; ++i) {
         const uint32_t j = c[i];
         const float d2 = dist2_vec4<PS>(qv, reinterpret_cast<const float4*>(points + static_cast<size_t>(j) * PS));
         tr.offer(make_key(d2, static_cast<int32_t>(j)));
     }
-    tr.emit(k, out_idx + static_cast<size_t>(q) * k, out_dist + static_cast<size_t>(q) * k);
+    tr.emit(k, out_idx + static_cast<size_t>(qi) * k, out_dist + static_cast<size_t>(qi) * k);
 }
 
 // Packs rows of float data ([rows][dims]) into the 128-byte-swizzle BF16 image of `tile`-row
@@ -298,14 +314,17 @@ __global__ void __launch_bounds__(128) tc_rescore_kernel(const float* __restrict
 // columns past `dims` are zero.
 __global__ void tc_pack_kernel(const float* __restrict__ src, uint32_t rows, uint32_t dims, uint32_t src_stride,
                                uint32_t tile, uint32_t H, uint8_t* __restrict__ img, float2* __restrict__ norms,
-                               uint32_t padded_rows) {
+                               uint32_t padded_rows, const uint32_t* __restrict__ order = nullptr,
+                               const uint32_t* __restrict__ live_count = nullptr) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= padded_rows) return;
     const uint32_t t = r / tile, rr = r % tile;
     uint8_t* base = img + static_cast<size_t>(t) * H * tile * 128u;
+    const bool valid = r < (live_count ? *live_count : rows);
+    const uint32_t sr = valid ? (order ? order[r] : r) : 0u;  // source row
     float acc = 0.0f;
     for (uint32_t k = 0; k < 64 * H; ++k) {
-        const float x = (r < rows && k < dims) ? src[static_cast<size_t>(r) * src_stride + k] : 0.0f;
+        const float x = (valid && k < dims) ? src[static_cast<size_t>(sr) * src_stride + k] : 0.0f;
         acc = __fmaf_rn(x, x, acc);
         const __nv_bfloat16 b = __float2bfloat16_rn(x);
         *reinterpret_cast<__nv_bfloat16*>(base + sw128_offset(tile, rr, k)) = b;
@@ -375,7 +394,8 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
 }
 
 size_t filter_smem(uint32_t H, uint32_t k) {
-    return 1024 + H * kTileM * 128u + 2 * H * kTileN * 128u + static_cast<size_t>(k) * kTileM * 4 + 16 * 8;
+    return 1024 + H * kTileM * 128u + 2 * H * kTileN * 128u + 2 * kTileN * sizeof(float2) +
+           static_cast<size_t>(k) * kTileM * 4 + 16 * 8;
 }
 
 // The filter allocates all 512 TMEM columns, so a second resident block on the same SM would
@@ -408,8 +428,8 @@ template <int PS, int KMAX>
 static int rescore(knn_index* ix, const QueryArgs& a, const uint32_t* cand, const uint32_t* cnt, uint32_t cap,
                    uint32_t* retry, uint32_t* retry_count, cudaStream_t s) {
     tc_rescore_kernel<PS, KMAX><<<ceil_div(a.count, 128), 128, 0, s>>>(
-        ix->points.as<float>(), a.queries, ix->dims, a.count, cand, cnt, cap, a.k, a.max_d2, a.radii, a.out_idx,
-        a.out_dist, retry, retry_count);
+        ix->points.as<float>(), a.queries, ix->dims, a.count, cand, cnt, cap, a.k, a.max_d2, a.radii, a.order,
+        a.count_dev, a.out_idx, a.out_dist, retry, retry_count);
     KNN_LAUNCHED();
     return KNN_OK;
 }
@@ -445,7 +465,8 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     uint32_t* retry = c.take<uint32_t>(nq);
     uint32_t* small = c.take<uint32_t>(64);  // [0] retry count, [1] error flag
     KNN_TRY_CUDA(cudaMemsetAsync(small, 0, 64 * sizeof(uint32_t), s));
-    tc_pack_kernel<<<ceil_div(qrows, 128), 128, 0, s>>>(a.queries, nq, ix->dims, ix->dims, kTileM, H, qimg, qnorm, qrows);
+    tc_pack_kernel<<<ceil_div(qrows, 128), 128, 0, s>>>(a.queries, nq, ix->dims, ix->dims, kTileM, H, qimg, qnorm, qrows,
+                                                        a.order, a.count_dev);
     KNN_LAUNCHED();
 
     TcParams p{};
@@ -462,6 +483,8 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     p.g = rel_margin(ix->dims);
     p.max_d2 = a.max_d2;
     p.radii = a.radii;
+    p.order = a.order;
+    p.live_count = a.count_dev;
     p.k = a.k;
     p.cap = cap;
     p.cand = cand;

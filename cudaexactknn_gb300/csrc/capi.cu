@@ -138,6 +138,9 @@ constexpr int kSeedRounds = 3;
 constexpr float kSeedGrowth = 16.0f;
 
 int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& plan, cudaStream_t s) {
+    // The tensor-core brute force tightens each query's bound from its own running upper bounds
+    // within the first tiles; a seed would only add retries, so it runs unseeded.
+    if (ix->structure == KNN_BRUTE_FORCE && plan.bf16) return dispatch(ix, a, plan, s);
     const size_t n = a.count;
     const uint32_t* order = nullptr;
     if (plan.reorder && a.count >= 4096) {
@@ -187,7 +190,8 @@ int k_slot(uint32_t k) {
 int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t s, knn::QueryPlan* out,
              float* best_ms, uint32_t* tried) {
     knn::QueryArgs t = a;
-    t.count = std::min<uint32_t>(a.count, 32768);
+    // Brute force costs n distances per query; a smaller sample keeps tuning short.
+    t.count = std::min<uint32_t>(a.count, ix->structure == KNN_BRUTE_FORCE ? 8192u : 32768u);
     t.counters = nullptr;
     cudaEvent_t e0, e1;
     KNN_TRY_CUDA(cudaEventCreate(&e0));
@@ -236,18 +240,25 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
                 if (rc != KNN_OK) break;
             }
             if (rc != KNN_OK) break;
-        } else if ((rc = consider(best)) != KNN_OK) {
-            break;
+        } else {
+            if ((rc = consider(best)) != KNN_OK) break;
+            // The BF16 tensor-core filter, for dims >= 16 (the brute-force form it is built for).
+            if (ix->dims >= 16 && knn::tc_supported(ix->dims, a.k)) {
+                knn::QueryPlan p = best;
+                p.bf16 = true;
+                if ((rc = consider(p)) != KNN_OK) break;
+            }
         }
         const knn::QueryPlan stage2 = best;
         for (uint32_t block : {32u, 64u, 256u}) {
+            if (stage2.bf16) break;  // the filter kernel has a fixed shape
             knn::QueryPlan p = stage2;
             p.block = block;
             if ((rc = consider(p)) != KNN_OK) break;
         }
         if (rc != KNN_OK) break;
         const knn::QueryPlan stage3 = best;
-        for (int v = 1; v < 8; ++v) {
+        for (int v = 1; v < 8 && !stage3.bf16; ++v) {
             knn::QueryPlan p = stage3;
             p.heap = v & 1;
             p.sh_nn = (v >> 1) & 1;
@@ -265,6 +276,19 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
     *tried = n_tried;
     return KNN_OK;
 }
+
+}  // namespace
+
+namespace knn {
+// The autotuner's plan for one query batch on one index (used by batches).
+int tune_plan(knn_index* ix, const QueryArgs& a, cudaStream_t s, QueryPlan* out) {
+    float ms = 0.0f;
+    uint32_t tried = 0;
+    return autotune(ix, a, false, s, out, &ms, &tried);
+}
+}  // namespace knn
+
+namespace {
 
 int run_query(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts, cudaStream_t s) {
     if (!ix) return fail(KNN_ERR_INVALID_ARGUMENT, "index is null");
@@ -473,6 +497,7 @@ int knn_tuned_plan(const knn_index* index, uint32_t k, uint32_t learned_radius, 
     out->shmem_stack = slot.plan.sh_stack;
     out->leaf_scan = slot.plan.leaf_scan;
     out->traversal = slot.plan.warp ? 1u : 0u;
+    out->flags = slot.plan.bf16 ? KNN_QF_BF16_FILTER : 0u;
     out->reserved = slot.candidates;
     if (ms) *ms = slot.ms;
     return KNN_OK;

@@ -12,6 +12,7 @@
 //   * k-th key cached in a register; tracker/stack storage chosen by the plan.
 
 #include <algorithm>
+#include <cstring>
 
 #include "tree_query.cuh"
 
@@ -34,7 +35,8 @@ struct KdParams {
     uint32_t dims;
     uint32_t nq;
     const uint32_t* order;  // thread -> query, or null
-    const uint32_t* count_dev;  // when set, *count_dev threads are live (nq is an upper bound)
+    const uint32_t* count_dev;
+    uint32_t order_base;  // subtracted from order entries (batched orders hold batch-wide ids)  // when set, *count_dev threads are live (nq is an upper bound)
     float max_d2;
     const float* radii;
     uint32_t k;
@@ -43,15 +45,13 @@ struct KdParams {
     DevCounters* counters;
 };
 
+// One thread's search: query slot t of the batch (its query is p.order[t] - p.order_base, or t).
 template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
-__global__ void __launch_bounds__(256) kd_knn_kernel(const KdParams p) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (p.count_dev ? *p.count_dev : p.nq)) return;  // no block-wide barriers below
+__device__ __forceinline__ void kd_search_thread(const KdParams& p, uint32_t t, unsigned char* smem) {
     uint64_t* sh_nn = reinterpret_cast<uint64_t*>(smem);
     uint32_t* sh_st = reinterpret_cast<uint32_t*>(smem + tracker_smem_bytes(SHNN, KMAX, blockDim.x));
 
-    const uint32_t qi = p.order ? p.order[t] : t;
+    const uint32_t qi = p.order ? p.order[t] - p.order_base : t;
     float q[DP];
     load_query<DP>(p.queries, p.dims, qi, q);
     const float r2 = p.radii ? p.radii[qi] : p.max_d2;
@@ -100,6 +100,14 @@ __global__ void __launch_bounds__(256) kd_knn_kernel(const KdParams p) {
     }
 }
 
+template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
+__global__ void __launch_bounds__(256) kd_knn_kernel(const KdParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (p.count_dev ? *p.count_dev : p.nq)) return;  // no block-wide barriers below
+    kd_search_thread<DP, KMAX, HEAP, SHNN, SHST>(p, t, smem);
+}
+
 // Warp-coherent variant: the 32 queries of a warp (neighbours after the leaf-order sort) walk the
 // tree together.  Each node's split is one broadcast load; the warp descends first into the
 // child most of its still-interested lanes are closer to; every lane keeps its own lower bound
@@ -107,18 +115,16 @@ __global__ void __launch_bounds__(256) kd_knn_kernel(const KdParams p) {
 // plane), and a subtree is skipped only when no lane's bound is within that lane's radius.
 // Leaf buckets are scanned by all lanes against the same slots (broadcast loads).  Control flow
 // is uniform across the warp; only the (rare) top-k insertions diverge.
+// One warp's search over slots t (this lane) of the batch; `live` slots exist.
 template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
-__global__ void __launch_bounds__(256) kd_knn_warp_kernel(const KdParams p) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t live = p.count_dev ? *p.count_dev : p.nq;
+__device__ __forceinline__ void kd_search_warp(const KdParams& p, uint32_t t, uint32_t live, unsigned char* smem) {
     const uint32_t warp_first = t & ~31u;
     if (warp_first >= live) return;  // whole warp idle; no block-wide barriers below
     const bool active = t < live;
     uint64_t* sh_nn = reinterpret_cast<uint64_t*>(smem);
     uint32_t* sh_st = reinterpret_cast<uint32_t*>(smem + tracker_smem_bytes(SHNN, KMAX, blockDim.x));
 
-    const uint32_t qi = active ? (p.order ? p.order[t] : t) : 0u;
+    const uint32_t qi = active ? (p.order ? p.order[t] - p.order_base : t) : 0u;
     float q[DP];
     load_query<DP>(p.queries, p.dims, qi, q);
     // Idle lanes (past the end of the batch) search with radius -1: they never want a node.
@@ -186,6 +192,14 @@ __global__ void __launch_bounds__(256) kd_knn_warp_kernel(const KdParams p) {
         lc.flush(p.counters);
         if (overflow) atomicExch(&p.counters->error, 1);
     }
+}
+
+template <int DP, int KMAX, bool HEAP, bool SHNN, bool SHST>
+__global__ void __launch_bounds__(256) kd_knn_warp_kernel(const KdParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t live = p.count_dev ? *p.count_dev : p.nq;
+    kd_search_warp<DP, KMAX, HEAP, SHNN, SHST>(p, t, live, smem);
 }
 
 // Sort key of a query: the node it reaches after `levels` closer-child steps (path bits).
@@ -300,5 +314,130 @@ int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStrea
 
 template int kd_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
 template int kd_order_dp<KNN_DP>(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
+
+
+// ---- batches of independent sets (one persistent kernel per class of sets) -----------------------
+struct KdBatchSet {
+    KdParams p;                 // the set's search parameters; p.order is the class order, p.order_base its offset
+    uint32_t first_block;  // first work block of this set in the class
+    uint32_t query_offset; // first query of this set in the class-wide numbering
+    uint32_t levels;       // descent depth of the locality key
+};
+
+__device__ __forceinline__ uint32_t kd_find_set(const KdBatchSet* sets, uint32_t nsets, uint32_t item, bool by_query) {
+    uint32_t lo = 0, hi = nsets;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if ((by_query ? sets[mid].query_offset : sets[mid].first_block) <= item) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Locality key of every query of the class: (set << 24) | descent path scaled to 24 bits.
+template <int DP>
+__global__ void kd_batch_key_kernel(const KdBatchSet* __restrict__ sets, uint32_t nsets, uint32_t total,
+                                     uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    const uint32_t si = kd_find_set(sets, nsets, g, true);
+    const KdParams& p = sets[si].p;
+    float q[DP];
+    load_query<DP>(p.queries, p.dims, g - sets[si].query_offset, q);
+    const uint32_t levels = sets[si].levels;
+    uint32_t node = 0;
+    for (uint32_t d = 0; d < levels; ++d) {
+        const float diff = pick<DP>(q, d % p.aux) - __ldg(p.split + node);
+        node = 2 * node + (diff < 0.0f ? 1u : 2u);
+    }
+    keys[g] = (si << 24) | ((node - ((1u << levels) - 1u)) << (24 - levels));
+    vals[g] = g;
+}
+
+// Persistent kernel: blocks take work blocks (blockDim queries of one set) from a shared counter
+// until the class is done; sets of very different sizes share the GPU without a launch each.
+template <int DP, int KMAX, bool WARP>
+__global__ void __launch_bounds__(256) kd_batch_kernel(const KdBatchSet* __restrict__ sets, uint32_t nsets,
+                                                        uint32_t total_blocks, uint32_t* __restrict__ counter) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint32_t item_s;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) item_s = atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t item = item_s;
+        if (item >= total_blocks) break;
+        const uint32_t si = kd_find_set(sets, nsets, item, false);
+        const KdParams& p = sets[si].p;
+        const uint32_t t = (item - sets[si].first_block) * blockDim.x + threadIdx.x;
+        if constexpr (WARP) {
+            kd_search_warp<DP, KMAX, false, false, false>(p, t, p.nq, smem);
+        } else {
+            if (t < p.nq) kd_search_thread<DP, KMAX, false, false, false>(p, t, smem);
+        }
+    }
+}
+
+template <uint32_t DP>
+int kd_batch_launch(const void* sets, uint32_t nsets, uint32_t total_queries, uint32_t total_blocks, uint32_t kmax,
+                       bool warp, uint32_t block, uint32_t* counter, uint32_t* keys, uint32_t* vals, bool key_pass,
+                       cudaStream_t s) {
+    using Set = KdBatchSet;
+    const Set* d_sets = static_cast<const Set*>(sets);
+    if (key_pass) {
+        kd_batch_key_kernel<DP><<<ceil_div(total_queries, 256), 256, 0, s>>>(d_sets, nsets, total_queries, keys, vals);
+        KNN_LAUNCHED();
+        return KNN_OK;
+    }
+#define KNN_BATCH(KM, W)                                                                              \
+    if (kmax == KM && warp == W) {                                                                    \
+        auto kern = kd_batch_kernel<DP, KM, W>;                                                    \
+        int per_sm = 0;                                                                               \
+        KNN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0));         \
+        const uint32_t grid = std::max(1, per_sm) * static_cast<uint32_t>(sm_count());                \
+        kern<<<std::min(grid, total_blocks), block, 0, s>>>(d_sets, nsets, total_blocks, counter);   \
+        KNN_LAUNCHED();                                                                               \
+        return KNN_OK;                                                                                \
+    }
+    KNN_BATCH(8, false) KNN_BATCH(16, false) KNN_BATCH(32, false) KNN_BATCH(64, false) KNN_BATCH(128, false)
+    KNN_BATCH(8, true) KNN_BATCH(16, true) KNN_BATCH(32, true) KNN_BATCH(64, true) KNN_BATCH(128, true)
+#undef KNN_BATCH
+    return fail(KNN_ERR_INVALID_ARGUMENT, "batch class k %u", kmax);
+}
+
+#if KNN_DP == 1
+// Fills the search parameters of one batch set from its index and item.
+size_t kd_batch_set_bytes() { return sizeof(KdBatchSet); }
+
+void kd_batch_set_fill(void* out, const knn_index* ix, const QueryArgs& a, const QueryPlan& plan,
+                        const uint32_t* order, uint32_t order_base, uint32_t first_block, uint32_t query_offset) {
+    KdBatchSet bs{};
+    KdParams& p = bs.p;
+    p.split = ix->split.as<float>();
+    p.aux = ix->aux_dims;
+    p.leaf = ix->leaf.as<float>();
+    p.leaf_stride = ix->leaf_stride;
+    p.node_count = ix->node_count;
+    p.node_depth = ix->node_depth;
+    p.stop_depth = scan_depth_for(ix->node_depth, ix->leaf_slots, plan.leaf_scan);
+    p.leaf_slots = ix->leaf_slots;
+    p.queries = a.queries;
+    p.dims = ix->dims;
+    p.nq = a.count;
+    p.order = order;
+    p.order_base = order_base;
+    p.max_d2 = a.max_d2;
+    p.k = a.k;
+    p.out_idx = a.out_idx;
+    p.out_dist = a.out_dist;
+    bs.first_block = first_block;
+    bs.query_offset = query_offset;
+    bs.levels = std::min<uint32_t>(ix->node_depth, 24);
+    std::memcpy(out, &bs, sizeof(bs));
+}
+#endif
+
+template int kd_batch_launch<KNN_DP>(const void*, uint32_t, uint32_t, uint32_t, uint32_t, bool, uint32_t, uint32_t*,
+                                      uint32_t*, uint32_t*, bool, cudaStream_t);
 
 }  // namespace knn

@@ -61,7 +61,7 @@ __device__ __forceinline__ void encode(const float* __restrict__ prm, const Mode
         float a = 0.0f;
         for (uint32_t d = 0; d < L.dims; ++d) a = fmaf(e[d], prm[L.proj + d * kFourier + f], a);
         float sv, cv;
-        sincosf(6.283185307179586f * a, &sv, &cv);
+        sincospif(2.0f * a, &sv, &cv);  // sin and cos of 2 pi a
         e[L.dims + f] = sv;
         e[L.dims + kFourier + f] = cv;
     }
@@ -169,8 +169,15 @@ __global__ void __launch_bounds__(256) mlp_infer_fast_kernel(const float* __rest
                                                              float* __restrict__ radii, float* __restrict__ raw) {
     extern __shared__ __align__(16) float sp[];
     const ModelLayout L(dims);
+    // sp: the parameters as stored, then W1 transposed ([feature][hidden]) for float4 loads.
+    float* w1t = sp + ((L.total + 3) & ~3u);
     for (uint32_t i = threadIdx.x; i < L.total; i += blockDim.x) sp[i] = prm[i];
+    for (uint32_t i = threadIdx.x; i < kHidden * L.feats; i += blockDim.x) {
+        const uint32_t h = i / L.feats, f = i % L.feats;
+        w1t[f * kHidden + h] = prm[L.w1 + i];
+    }
     __syncthreads();
+    const float4* w1t4 = reinterpret_cast<const float4*>(w1t);
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= count) return;
     float z[DP];
@@ -182,11 +189,19 @@ __global__ void __launch_bounds__(256) mlp_infer_fast_kernel(const float* __rest
     float h1[kHidden];
 #pragma unroll
     for (int i = 0; i < static_cast<int>(kHidden); ++i) h1[i] = sp[L.b1 + i];
+    auto add_feature = [&](uint32_t f, float v) {
+#pragma unroll
+        for (int i4 = 0; i4 < static_cast<int>(kHidden / 4); ++i4) {
+            const float4 w = w1t4[f * (kHidden / 4) + i4];
+            h1[4 * i4 + 0] = fmaf(w.x, v, h1[4 * i4 + 0]);
+            h1[4 * i4 + 1] = fmaf(w.y, v, h1[4 * i4 + 1]);
+            h1[4 * i4 + 2] = fmaf(w.z, v, h1[4 * i4 + 2]);
+            h1[4 * i4 + 3] = fmaf(w.w, v, h1[4 * i4 + 3]);
+        }
+    };
 #pragma unroll
     for (int d = 0; d < DP; ++d)
-        if (static_cast<uint32_t>(d) < dims)
-#pragma unroll
-            for (int i = 0; i < static_cast<int>(kHidden); ++i) h1[i] = fmaf(sp[L.w1 + i * L.feats + d], z[d], h1[i]);
+        if (static_cast<uint32_t>(d) < dims) add_feature(d, z[d]);
 #pragma unroll 1
     for (uint32_t f = 0; f < kFourier; ++f) {
         float a = 0.0f;
@@ -194,12 +209,9 @@ __global__ void __launch_bounds__(256) mlp_infer_fast_kernel(const float* __rest
         for (int d = 0; d < DP; ++d)
             if (static_cast<uint32_t>(d) < dims) a = fmaf(z[d], sp[L.proj + d * kFourier + f], a);
         float sv, cv;
-        sincosf(6.283185307179586f * a, &sv, &cv);
-#pragma unroll
-        for (int i = 0; i < static_cast<int>(kHidden); ++i) {
-            h1[i] = fmaf(sp[L.w1 + i * L.feats + dims + f], sv, h1[i]);
-            h1[i] = fmaf(sp[L.w1 + i * L.feats + dims + kFourier + f], cv, h1[i]);
-        }
+        sincospif(2.0f * a, &sv, &cv);
+        add_feature(dims + f, sv);
+        add_feature(dims + kFourier + f, cv);
     }
 #pragma unroll
     for (int i = 0; i < static_cast<int>(kHidden); ++i) h1[i] = fmaxf(h1[i], 0.0f);
@@ -356,10 +368,12 @@ int model_gradients(const float* d_prm, uint32_t dims, const float* d_x, const f
 int model_predict(const float* d_prm, uint32_t dims, const float* d_x, uint32_t count, float max_d2,
                   const float* user_radii, float* d_radii, float* d_raw, cudaStream_t s) {
     const ModelLayout L(dims);
-    const size_t smem = static_cast<size_t>(L.total) * sizeof(float);
+    const size_t smem = (static_cast<size_t>((L.total + 3) & ~3u) + kHidden * L.feats) * sizeof(float);
     const bool aligned = (L.w2 % 4) == 0;
 #define KNN_INFER(D_)                                                                                     \
     if (aligned && dims <= D_) {                                                                          \
+        KNN_TRY_CUDA(cudaFuncSetAttribute(mlp_infer_fast_kernel<D_>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                          static_cast<int>(smem)));                                       \
         mlp_infer_fast_kernel<D_><<<ceil_div(count, 256), 256, smem, s>>>(d_prm, dims, d_x, count, max_d2, \
                                                                           user_radii, d_radii, d_raw);    \
         KNN_LAUNCHED();                                                                                   \

@@ -250,6 +250,54 @@ class BallTreeGpu(_Index):
                                                _stream_handle(stream), ctypes.byref(self._h)))
 
 
+class Batch:
+    """Many (tree, query batch) pairs answered by one CUDA-graph launch (knn_batch_create/run).
+
+    ``items`` is a list of ``(index, queries, k, max_distance2)``; the result tensors are made
+    here and reused by every ``run``.  Refill the query tensors in place between runs: their
+    addresses are part of the captured graph.  The reference answers each pair with its own
+    batchKnn call (src/KdTreeGpu.cuh:392-410, src/BallTreeGpu.cuh:630-648)."""
+
+    def __init__(self, items, autotune: bool = False, keep_order: bool = False, stream=None):
+        self._h = ctypes.c_void_p()
+        self.items = []
+        arr = (_lib.BatchItem * max(1, len(items)))()
+        for j, (ix, queries, k, r2) in enumerate(items):
+            q = _check_points(queries, "queries")
+            if q.shape[1] != ix.dims:
+                raise ValueError(f"item {j}: queries have {q.shape[1]} dims, the index {ix.dims}")
+            oi = torch.empty((q.shape[0], k), dtype=torch.int32, device=q.device)
+            od = torch.empty((q.shape[0], k), dtype=torch.float32, device=q.device)
+            self.items.append((ix, q, oi, od))
+            arr[j] = _lib.BatchItem(ix.handle.value, q.data_ptr(), q.shape[0], r2, k, oi.data_ptr(), od.data_ptr())
+        flags = (_lib.QF_AUTOTUNE if autotune else 0) | (_lib.QF_KEEP_ORDER if keep_order else 0)
+        _lib.check(_lib.load().knn_batch_create(arr, len(items), flags, _stream_handle(stream), ctypes.byref(self._h)))
+
+    def run(self, sync: bool = True, stream=None):
+        """Answers every item; returns [(indexes, distances)] in item order."""
+        _lib.check(_lib.load().knn_batch_run(self._h, _stream_handle(stream)))
+        if sync:
+            (stream or torch.cuda.current_stream()).synchronize()
+        return [(oi, od) for _, _, oi, od in self.items]
+
+    def info(self) -> tuple[int, int]:
+        """(classes, kernel launches per run)."""
+        c, k = ctypes.c_uint32(), ctypes.c_uint32()
+        _lib.check(_lib.load().knn_batch_info(self._h, ctypes.byref(c), ctypes.byref(k)))
+        return c.value, k.value
+
+    def close(self) -> None:
+        if self._h:
+            _lib.load().knn_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def build_index(structure: str, points: torch.Tensor, depth_skips: int | None = None, **kw) -> _Index:
     if structure == "bf":
         return BruteForceGpu(points, **kw)

@@ -177,6 +177,30 @@ KNN_API int knn_query_stats(knn_index* index, const float* d_queries, uint32_t c
                     float max_distance2, uint32_t k, int32_t* d_indexes, float* d_distances,
                     const knn_query_opts* opts, void* stream, knn_query_counters* out);
 
+/* ---- batches of independent sets (the reference answers one set per batchKnn call, each ending in
+ *      a device-wide sync: src/KdTreeGpu.cuh:393-410, src/BallTreeGpu.cuh:631-648) ---------------- */
+typedef struct knn_batch knn_batch;
+typedef struct knn_batch_item {
+    knn_index* index;         /* k-d or ball tree */
+    const float* d_queries;   /* [count][dims], device */
+    uint32_t count;
+    float max_distance2;
+    uint32_t k;
+    int32_t* d_indexes;       /* [count][k], device */
+    float* d_distances;       /* [count][k], device */
+} knn_batch_item;
+/* Plans a batch: items grouped by (tree, dims, k) class, one persistent kernel per class over all
+ * its sets, the classes captured as parallel branches of one CUDA graph.  flags: KNN_QF_AUTOTUNE
+ * tunes each class on its largest set (runs queries, synchronously); KNN_QF_KEEP_ORDER skips the
+ * locality sort.  The items' pointers are baked into the graph: refill the buffers, not the items. */
+KNN_API int knn_batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, void* stream,
+                             knn_batch** out);
+/* Runs every item of the batch: one cudaGraphLaunch on `stream`. */
+KNN_API int knn_batch_run(knn_batch* batch, void* stream);
+/* Classes in the batch and kernel launches one knn_batch_run makes (kernel nodes of its graph). */
+KNN_API int knn_batch_info(const knn_batch* batch, uint32_t* classes, uint32_t* kernels_per_run);
+KNN_API int knn_batch_destroy(knn_batch* batch);
+
 /* ---- learned radius (no counterpart in the reference; it seeds Query::maxDistance2,
  *      src/KnnTrees.cuh:228, per query) ---------------------------------------------------------
  * Trains the index's D->64->64->1 radius model on `count` sample queries (device float32
