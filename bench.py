@@ -52,7 +52,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (debug only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-once", choices=["chosen", "plain"], default=None,
@@ -219,8 +219,175 @@ def cpu_baseline(w, threads, sample=None):
     return len(qs) / dt, build_s, len(qs)
 
 
+PLAIN_KW = {"kd": dict(block_size=32, shmem_stack=True),
+            "ball": dict(block_size=16, heap=True, shmem_tracking=True, shmem_stack=True),
+            "bf": dict(block_size=32)}
+
+
+def run_reference_c5(args):
+    """The reference's CPU trees on every set of the uneven batch (a sample of each set's queries)."""
+    import oracle
+    threads = os.cpu_count() or 1
+    sets = W.c5_sets(args.scale)
+    trees = [(oracle.kd_tree(w.points, w.depth_skips) if w.structure == "kd" else
+              oracle.ball_tree(w.points, w.depth_skips), w) for w in sets]
+    per_set = 256
+
+    def step():
+        for tree, w in trees:
+            tree.knn(w.queries[:per_set], w.k, w.max_dist2, fma=True, strict=False, threads=threads)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    nq = sum(min(per_set, len(w.queries)) for w in sets)
+    qps = nq * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "c5_uneven_batch_64_sets", "structure": "KdTree<3|8> / BallTree<32> (CPU)",
+                   "queries_per_step": nq},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"first {per_set} queries of each of the {len(sets)} sets per step, oracle "
+                                   f"port of src/KdTree.cuh and src/BallTree.cuh, {threads} host threads"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_c5(args, world, rank, local):
+    """Uneven batch: 64 independent sets, one plain batchKnn per set (each ending in a device
+    synchronisation, as the reference's does) against one graph launch of the whole batch."""
+    import torch
+    from cudaexactknn_gb300 import _lib, knn
+    import oracle
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+    sets = W.c5_sets(args.scale)
+    built = []
+    for w in sets:
+        ix = knn.build_index(w.structure, torch.from_numpy(w.points).to(dev), w.depth_skips)
+        q = torch.from_numpy(w.queries).to(dev)
+        built.append((w, ix, knn.Query(q, len(w.queries), w.max_dist2)))
+    total_q = sum(len(w.queries) for w in sets)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def plain_step():
+        for w, ix, q in built:
+            ix.batch_knn(q, w.k, **PLAIN_KW[w.structure])
+
+    batch = knn.Batch([(ix, q.points, w.k, w.max_dist2) for w, ix, q in built], autotune=True)
+    classes, kernels_per_run = batch.info()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        ms = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            ms += a.elapsed_time(b)
+        barrier(world)
+        return max_over_ranks(world, ms)
+
+    launches0 = lib.knn_launch_count()
+    with ClockSampler(local) as clocks:
+        chosen_ms = timed(lambda: batch.run(sync=False), args.steps, args.warmup)
+    graph_launches = lib.knn_launch_count() - launches0
+    plain_ms = timed(plain_step, args.steps, max(1, args.warmup // 2))
+    value = world * total_q * args.steps / (chosen_ms / 1e3)
+    plain_qps = world * total_q * args.steps / (plain_ms / 1e3)
+
+    # Exactness: a sample of every set's rows from the batch against the oracle's brute force.
+    rows_ok = rows = 0
+    plain_ok = 0
+    res = batch.run()
+    rng = np.random.default_rng(0)
+    for (w, ix, q), (oi, od) in zip(built, res):
+        pick = rng.choice(len(w.queries), size=min(64, len(w.queries)), replace=False)
+        want = oracle.row_keys(*oracle.bf_knn(w.points, w.queries[pick], w.k, w.max_dist2, fma=True,
+                                              threads=os.cpu_count() or 1))
+        got = oracle.row_keys(oi[pick].cpu().numpy(), od[pick].cpu().numpy())
+        rows_ok += int((got == want).all(axis=1).sum())
+        pi, pd = ix.batch_knn(q, w.k, **PLAIN_KW[w.structure])
+        plain_ok += int((oracle.row_keys(pi[pick].cpu().numpy(), pd[pick].cpu().numpy()) == want).all(axis=1).sum())
+        rows += len(pick)
+
+    # End to end: pinned host queries in, the graph launch, every result out.
+    h_q = [torch.from_numpy(w.queries).pin_memory() for w, _, _ in built]
+    h_out = [(torch.empty(oi.shape, dtype=torch.int32).pin_memory(), torch.empty(od.shape).pin_memory())
+             for oi, od in res]
+
+    def e2e_step():
+        for (w, ix, q), hq in zip(built, h_q):
+            q.points.copy_(hq, non_blocking=True)
+        batch.run(sync=False)
+        for (oi, od), (hi, hd) in zip(res, h_out):
+            hi.copy_(oi, non_blocking=True)
+            hd.copy_(od, non_blocking=True)
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_s += time.perf_counter() - t0
+    e2e_s = max_over_ranks(world, e2e_s)
+
+    # Roofline: bytes the batch must move (every set's points, queries and result rows once)
+    # over the batch time -- the compulsory traffic, HBM bound.
+    compulsory = sum(w.points.nbytes + w.queries.nbytes + len(w.queries) * w.k * 8 for w in sets)
+    peak, peak_kind = peaks()
+    achieved = compulsory / (chosen_ms / args.steps / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": chosen_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, shapes of the config)",
+        "config": {"workload": "c5_uneven_batch_64_sets", "sets": len(sets), "queries": total_q,
+                   "points": int(sum(len(w.points) for w in sets)), "classes": classes,
+                   "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
+        "exact_match": {"chosen": rows_ok / rows, "plain": plain_ok / rows, "sample_queries": rows},
+        "plain": {"value": plain_qps, "ms_per_step": plain_ms / args.steps,
+                  "form": "one batchKnn per set with the reference benchmarks' template choices"},
+        "chosen": {"form": "one CUDA-graph launch, one persistent kernel per (tree, dims, k) class, autotuned",
+                   "kernels_per_run": kernels_per_run, "speedup_vs_plain": value / plain_qps},
+        "e2e": {"value": world * total_q * args.steps / e2e_s, "unit": "queries/s",
+                "h2d_bytes_per_step": int(sum(w.queries.nbytes for w in sets)),
+                "d2h_bytes_per_step": int(sum(len(w.queries) * w.k * 8 for w in sets))},
+        "gpu_launches": int(kernels_per_run * args.steps),
+        "graph_launches": int(graph_launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": f"{peak_kind} hbm_gbs", "kernel": "kd/ball_batch_kernel",
+                     "algorithmic_bytes_per_launch": int(compulsory)},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    batch.close()
+
+
 def run_reference(args, world, rank):
     if rank != 0:
+        return
+    if args.workload == "c5":
+        run_reference_c5(args)
         return
     w = workload(args)
     threads = os.cpu_count() or 1
@@ -270,6 +437,10 @@ def main():
         run_reference(args, world, rank)
         return
 
+    if args.workload == "c5":
+        run_c5(args, world, rank, local)
+        return
+
     import ctypes
     import torch
     from cudaexactknn_gb300 import _lib, knn
@@ -294,8 +465,7 @@ def main():
     # Plain form: the reference benchmarks' template choices (kd <K,32,false,false,true>,
     # ball <K,16,true,true,true>, brute force <K,32,false,false>; tests/Dim3SpeedTests.cu:38,43,
     # tests/DimXSpeedTests.cu:52), no autotune, no learned radius.
-    plain_kw = {"kd": dict(block_size=32, shmem_stack=True), "ball": dict(block_size=16, heap=True,
-                shmem_tracking=True, shmem_stack=True), "bf": dict(block_size=32)}[w.structure]
+    plain_kw = PLAIN_KW[w.structure]
     # Chosen form: the engine's autotuned plan seeded by the learned radius.
     train = w.extra.get("train")
     report = None

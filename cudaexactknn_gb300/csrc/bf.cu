@@ -36,8 +36,6 @@ int bf_build(knn_index* ix, const float* d_points, cudaStream_t s) {
 }
 
 int bf_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s) {
-    // The tensor-core filter where its tile fits (k <= 100 at dims > 64), else the SIMT kernel.
-    if (p.bf16 && tc_supported(ix->dims, a.k)) return bf_tc_query(ix, a, p, s);
     switch (ix->dp) {
         case 1: return bf_query_dp<1>(ix, a, p, s);
         case 2: return bf_query_dp<2>(ix, a, p, s);

@@ -35,7 +35,9 @@ __global__ void __launch_bounds__(256) bf_knn_kernel(const BfParams p) {
     uint64_t* sh_nn = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(p.tile) * PS * sizeof(float));
 
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = t < (p.count_dev ? *p.count_dev : p.nq);
+    const uint32_t live = p.count_dev ? *p.count_dev : p.nq;
+    if (blockIdx.x * blockDim.x >= live) return;  // the whole block is past the live list
+    const bool active = t < live;
     const uint32_t qi = active ? (p.order ? p.order[t] : t) : 0u;
     float q[PS];
 #pragma unroll

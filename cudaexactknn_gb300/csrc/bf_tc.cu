@@ -1,38 +1,66 @@
-// Brute force with a BF16 tensor-core filter (tcgen05, sm_103a) and exact FP32 rescoring.
+// Exact kNN through a 16-bit tensor-core filter (tcgen05, sm_103a) with cell skipping and exact
+// FP32 rescoring, for any index (brute force, k-d tree, ball tree).
 //
-// The reference computes every pair's distance with SIMT FP32 (src/BruteForceGpu.cuh:9-31).
-// For dims >= 16 the engine can instead compute G = q~ . p~ for all pairs as a BF16 GEMM with FP32
-// accumulation on the 5th-generation tensor cores, and use
-//     |q|^2 + |p|^2 - 2 G  +-  E(q, p)
-// as a rigorous interval around each pair's distance.  The lower end filters candidates, the
-// upper end maintains each query's running k-th bound T; every candidate is then rescored with
-// the reference's own sequential FP32 sum, so the answer is exactly the plain brute force's.
+// The reference computes every pair's distance with SIMT FP32 (src/BruteForceGpu.cuh:9-31) or
+// walks a tree per query (src/KdTreeGpu.cuh:392-410, src/BallTreeGpu.cuh:630-648).  Here:
 //
-// Error bound (u = 2^-8 is bf16's unit roundoff; q~, p~ are q, p rounded to bf16):
-//   |q~_d p~_d - q_d p_d| <= (2u + u^2) |q_d p_d|,  sum |q_d p_d| <= |q| |p|  (Cauchy-Schwarz),
-//   tensor-core FP32 accumulation of D products <= D 2^-20 sum |q~_d p~_d|  (8x the bound for
-//   truncating every addition),
-//   norms |q|^2, |p|^2 in float: relative error <= (D+1) 2^-24,
-// so with S = exact sum (q_d - p_d)^2:
-//   |(|q|^2 + |p|^2 - 2G) - S| <= c1 |q||p| + c2 (|q|^2 + |p|^2),
-//   c1 = 2 (2u + u^2 + D 2^-20)(1 + 2^-7),  c2 = (D + 8) 2^-23.
-// The float sequential sum S_f the engine reports satisfies S (1 - g) <= S_f <= S (1 + g) with
-// g = (D + 4) 2^-23 (knn::rel_margin).  A point is a candidate when (lower bound)(1 - g) <= T; T is
-// the k-th smallest (upper bound)(1 + g) seen so far, which is >= the final k-th S_f, so every
-// point that can enter the top-k (ties included) is a candidate.
+// Layout, once per index.  Landmarks (every (n/L)-th point, L about n/1024; cells much wider
+// than the median cell get a second landmark at their farthest point, twice) split the points
+// into Voronoi cells.  The points are laid out cell by cell in tiles of 256 rows, each cell's last
+// tile padded.  Every cell gets a centre (the mean of its points) and a radius bounding the
+// exact distance from the centre to each of its points.  The operand images hold every row, and
+// every cell centre, scaled by s = 2^e (e >= 0, largest |coordinate| * s in [2^13, 2^14)) and
+// rounded to FP16; data whose largest |coordinate| exceeds 2^14 uses BF16 with s = 1.
 //
-// Kernel shape: one CTA per 128 queries, 6 warps: warp 0 streams 256-point BF16 tiles into a
-// 2-stage shared-memory ring with bulk asynchronous copies, warp 1 allocates tensor memory and
-// issues tcgen05.mma (M=128, N=256, K=16 steps) into two TMEM accumulators of 256 columns,
-// warps 2-5 read accumulator rows with tcgen05.ld (thread = query) and filter.  Operands are
-// pre-packed in global memory in the exact shared-memory image of the K-major 128-byte-swizzle
-// layout, so plain bulk copies (no tensor maps) land them ready for the MMA descriptors.
+// Per query batch.  Each query goes to its nearest landmark's cell and the batch is sorted by
+// cell.  A run of 128 sorted queries (a query tile) has a home range: the cells of its queries,
+// widened by whole cells to at least max(2k, 512) points.  One CTA per query tile, over a
+// sequence of 256-row tiles:
+//   phase 1   the home tiles: each query's running k-th upper bound T;
+//   centres   the cell-centre tiles: per query and cell, a rigorous lower bound on the distance
+//             from the query to any point of the cell (the GEMM bound below, less the radius);
+//             a cell is kept when some query of the tile may need it;
+//   phase 2   the tiles of every kept cell outside the home range.
+// Per tile, warp 1 issues tcgen05.mma (M = 128 queries, N = 256 rows, K = 16 per step over the
+// padded dims) into one of two TMEM accumulators, warp 0 streams the operand tile and its row data
+// by bulk asynchronous copy, and warps 2-5 read accumulator rows (thread = query).  The exact
+// rescoring then ranks the candidates by the reference's own sequential FP32 squared-difference
+// sum, so every answer is the plain search's.  Queries whose candidates overflow the list, or that
+// the 16-bit format cannot hold, take the plain search.
+//
+// GEMM bound.  q', p' are scaled FP32 vectors (exact: s is a power of two >= 1), u the format's
+// unit roundoff (2^-11 FP16, 2^-8 BF16), delta the largest absolute rounding error of a value in
+// the subnormal range (2^-14 for FP16, which also covers flushing to zero; negligible for BF16).
+// With G the FP32-accumulated tensor-core sum of the rounded products:
+//   |G - q'.p'| <= E = c1 |q'||p'| + c3 (|q'| + |p'|) + c4,
+//   c1 = (2u + u^2 + D 2^-20 (1+u)^2)(1 + 2^-10),  c3 = 1.01 delta (1+u) sqrt(D),
+//   c4 = 1.01 D delta^2 + 2 s^2 (D+4) 2^-149   (the last term: float distances in the subnormal range)
+// (product rounding summed by Cauchy-Schwarz; FP32 accumulation of D products within D 2^-20 of
+// their magnitude sum, 8x the bound for truncating every addition).  The float norms n = fl(|x'|^2)
+// have relative error below gn = (D+4) 2^-23, so the exact scaled distance S' = s^2 S obeys
+//   (1-gn)(n_q + n_p) - 2G - 2E  <=  S'  <=  (1+gn)(n_q + n_p) - 2G + 2E,
+// and the engine's float distance S_f obeys S (1-g) <= S_f <= S (1+g), g = (D+4) 2^-23.
+//
+// Candidate test (point tiles).  With Pmax >= |p'| over the tile, a point can be among a query's k
+// nearest (ties included) only if
+//   G - a n_p  >=  a n_q - E(Pmax) - T' / (2 (1-g)),    a = (1-gn)/2,
+// where T' is the k-th smallest upper bound (1+g)((1+gn)(n_q+n_p) - 2G + 2E(Pmax)) seen so far.
+// The epilogue rounds the left side up (one FMA) and the right side down (once per tile and per
+// change of T'), so the filter can only keep extra candidates.
+//
+// Cell test (centre tiles).  For a cell of centre c' and radius R' (scaled), every point p' of it
+// has |q' - p'| >= |q' - c'| - R', so no point of the cell can reach a query's k nearest when
+//   S_lo = (1-gn)(n_q + n_c) - 2G - 2E(Cmax)  >  (R' + t)^2,   t >= sqrt((T' + c4) / (1 - g)).
+// The left side is rounded down and the right side up.
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <numeric>
 #include <vector>
 
 #include "knn_internal.h"
@@ -50,29 +78,51 @@ constexpr uint32_t kTileN = 256;
 constexpr uint32_t kEpiWarps = 4;
 constexpr uint32_t kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kTmemCols = 512;  // two accumulators of kTileN fp32 columns
+constexpr uint32_t kCellPoints = 1024;
+constexpr uint32_t kMaxCells = 4096;
+constexpr uint32_t kMaskWords = kMaxCells / 32;
+constexpr uint32_t kRowData = 2 * kTileN;  // floats of row data per tile: norms, then (centres) radii
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+
+__host__ __device__ __forceinline__ uint32_t a_bytes(uint32_t h) { return h * kTileM * 128u; }
+__host__ __device__ __forceinline__ uint32_t b_bytes(uint32_t h) { return h * kTileN * 128u; }
+
+// Constants of the GEMM bound (scaled units).
+struct Bounds {
+    float c1, c3, c4;  // |G - q'.p'| <= c1 |q'||p'| + c3 (|q'| + |p'|) + c4
+    float gn;          // relative error of the float norms
+    float g;           // relative error of the engine's float distance
+    float inv_one_m;   // >= 1 / (1 - g)
+};
 
 struct TcParams {
-    const uint8_t* qimg;  // [qtiles][H][128 rows][128 B]
-    const uint8_t* pimg;  // [ptiles][H][256 rows][128 B]
-    const float2* qnorm;  // per query: {|q|^2, |q|}
-    const float2* pnorm;  // per point: {|p|^2, |p|}
-    uint32_t n, nq, ptiles;
-    float c1, c2, g;
-    float max_d2;
-    const float* radii;   // per-query radius or null (indexed by query)
-    const uint32_t* order;       // row -> query, or null
+    const uint8_t* qimg;         // [qtiles][H][128 rows][128 B]
+    const uint8_t* pimg;         // [ptiles][H][256 rows][128 B]
+    const uint8_t* cimg;         // [ctiles][H][256 rows][128 B] cell centres
+    const float* qnorm;          // per query row: n_q (NaN: not representable, plain search)
+    const float* pnorm;          // per padded point row: n_p (+inf on padding rows)
+    const float* cdata;          // per centre tile: 256 norms (+inf past the last cell), 256 radii
+    const float* pmax;           // per point tile: >= |p'|
+    const float* cmax;           // per centre tile: >= |c'|
+    const uint32_t* cell_tile;   // [cells + 1] first point tile of each cell
+    const uint32_t* qhome;       // per query tile: first tile, end tile, first cell, last cell
+    uint32_t cells, ctiles, nq, ksteps, idesc;
+    Bounds b;
+    float s2, max_d2;
+    const float* radii;          // per query index, or null
+    const float* seed;           // per query index: an upper bound on its k-th float distance
+    const uint32_t* order;       // row -> query index
     const uint32_t* live_count;  // rows in use (device), or null for nq
-    uint32_t k;
-    uint32_t cap;
-    uint32_t* cand;       // [nq][cap]
-    uint32_t* cand_count; // [nq]
+    uint32_t k, cap;
+    uint32_t* cand;              // [nq][cap] padded point rows
+    float* cand_v;               // [nq][cap] their tensor-core sums G
+    uint32_t* cand_count;        // [nq]; kNone = plain search
+    float* final_t;              // [nq] the row's k-th upper bound T' after the last tile
+    DevCounters* counters;
     int* error;
 };
 
-__device__ __forceinline__ uint32_t a_bytes(uint32_t h) { return h * kTileM * 128u; }
-__device__ __forceinline__ uint32_t b_bytes(uint32_t h) { return h * kTileN * 128u; }
-
-// Heap of this thread's k smallest upper bounds (max at slot 0), slot-major in shared memory.
+// Heap of a thread's k smallest upper bounds (max at slot 0), slot-major in shared memory.
 struct BoundHeap {
     float* base;  // slot i at base[i * kTileM]
     uint32_t k;
@@ -96,6 +146,63 @@ struct BoundHeap {
     }
 };
 
+// The tile sequence of a query tile, identical for every role: home tiles [t0, t1), the centre
+// tiles, then (after the mask is complete) the tiles of each kept cell outside [c0, c1].
+struct TileSeq {
+    uint32_t t0, t1, c0, c1, cells, ctiles;
+    const uint32_t* mask;       // shared memory, kMaskWords words
+    const uint32_t* cell_tile;  // global
+    uint32_t stage = 0;         // 0 home, 1 centres, 2 kept cells
+    uint32_t t = 0, tend = 0, word = 0, bits = 0;
+    // Next item; *centre tells the kind.  Returns false at the end of stages 0-1 (the caller
+    // then starts the next stage) and at the very end.
+    __device__ __forceinline__ bool next(uint32_t* item, bool* centre) {
+        if (stage == 0) {
+            if (t < t1) {
+                *item = t++;
+                *centre = false;
+                return true;
+            }
+            return false;
+        }
+        if (stage == 1) {
+            if (t < ctiles) {
+                *item = t++;
+                *centre = true;
+                return true;
+            }
+            return false;
+        }
+        while (t >= tend) {
+            while (bits == 0) {
+                if (++word >= kMaskWords || word * 32 >= cells) return false;
+                bits = mask[word];
+            }
+            const uint32_t c = word * 32 + static_cast<uint32_t>(__ffs(bits) - 1);
+            bits &= bits - 1u;
+            if (c >= cells) return false;
+            if (c >= c0 && c <= c1) continue;
+            t = __ldg(cell_tile + c);
+            tend = __ldg(cell_tile + c + 1);
+        }
+        *item = t++;
+        *centre = false;
+        return true;
+    }
+    __device__ __forceinline__ void begin(uint32_t st) {
+        stage = st;
+        if (st == 0) t = t0;
+        if (st == 1) t = 0;
+        if (st == 2) {
+            t = tend = 0;
+            word = 0;
+            bits = mask[0];
+        }
+    }
+};
+
+__device__ __forceinline__ void epilogue_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(kEpiWarps * 32) : "memory"); }
+
 template <uint32_t H>
 __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p) {
     extern __shared__ uint8_t smem_raw[];
@@ -103,22 +210,35 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     const uint32_t raw = smem_addr(smem_raw);
     uint8_t* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
     uint8_t* sA = smem;
-    uint8_t* sB0 = sA + H * kTileM * 128u;
-    uint8_t* sB1 = sB0 + H * kTileN * 128u;
-    float2* sN = reinterpret_cast<float2*>(sB1 + H * kTileN * 128u);  // [2][kTileN] point norms
-    float* heap_base = reinterpret_cast<float*>(sN + 2 * kTileN);
+    uint8_t* sB0 = sA + a_bytes(H);
+    uint8_t* sB1 = sB0 + b_bytes(H);
+    float* sN = reinterpret_cast<float*>(sB1 + b_bytes(H));       // [2][kRowData] row data
+    uint32_t* sMask = reinterpret_cast<uint32_t*>(sN + 2 * kRowData);  // [kMaskWords] kept cells
+    float* heap_base = reinterpret_cast<float*>(sMask + kMaskWords);   // [k][kTileM]
     uint64_t* bars = reinterpret_cast<uint64_t*>(heap_base + static_cast<size_t>(p.k) * kTileM);
-    uint64_t* full = bars;         // [2] B stage loaded
-    uint64_t* empty = bars + 2;    // [2] B stage consumed by the MMAs
-    uint64_t* acc_full = bars + 4; // [2] accumulator ready
-    uint64_t* acc_empty = bars + 6;// [2] accumulator drained by the epilogue
-    uint64_t* a_full = bars + 8;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 9);
+    uint64_t* full = bars;            // [2] tile (operands + row data) landed
+    uint64_t* empty = bars + 2;       // [2] operands consumed by the MMAs
+    uint64_t* acc_full = bars + 4;    // [2] accumulator ready
+    uint64_t* acc_empty = bars + 6;   // [2] accumulator and row data drained by the epilogue
+    uint64_t* a_full = bars + 8;      // query tile landed
+    uint64_t* mask_ready = bars + 9;  // kept-cell mask complete
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 10);
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const uint32_t live_rows = p.live_count ? *p.live_count : p.nq;
-    if (blockIdx.x * kTileM >= live_rows) return;  // whole block idle: leave before any allocation
+    const uint32_t qt = blockIdx.x;
+    if (qt * kTileM >= live_rows) return;  // whole block idle: leave before any allocation
+    TileSeq seq;
+    seq.t0 = p.qhome[4 * qt];
+    seq.t1 = p.qhome[4 * qt + 1];
+    seq.c0 = p.qhome[4 * qt + 2];
+    seq.c1 = p.qhome[4 * qt + 3];
+    seq.cells = p.cells;
+    seq.ctiles = p.ctiles;
+    seq.mask = sMask;
+    seq.cell_tile = p.cell_tile;
+    for (uint32_t w = threadIdx.x; w < kMaskWords; w += blockDim.x) sMask[w] = 0;
     if (threadIdx.x == 0) {
         for (int i = 0; i < 2; ++i) {
             mbar_init(full + i, 1);
@@ -127,6 +247,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
             mbar_init(acc_empty + i, kEpiWarps * 32);
         }
         mbar_init(a_full, 1);
+        mbar_init(mask_ready, kEpiWarps * 32);
         *abort = 0;
         mbar_fence_init();
     }
@@ -135,136 +256,255 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t ptiles = p.ptiles;
 
     if (warp == 0) {
         if (lane == 0) {
-            // Producer: the query tile once, then the point tiles through the 2-stage ring.
+            // Producer: the query tile once, then the tile sequence through the 2-stage ring.
             mbar_expect_tx(a_full, a_bytes(H));
-            bulk_copy_g2s(sA, p.qimg + static_cast<size_t>(blockIdx.x) * a_bytes(H), a_bytes(H), a_full);
-            uint32_t issued = 0;
-            constexpr uint32_t kNormBytes = kTileN * sizeof(float2);
-            for (uint32_t t = 0; t < ptiles; ++t) {
-                const uint32_t s = t & 1;
-                // Stage s is free once the MMAs of tile t-2 are done (operands) and the epilogue
-                // has drained tile t-2 (its norms).
-                if (t >= 2 && (!mbar_wait(empty + s, ((t >> 1) - 1) & 1, abort) ||
-                               !mbar_wait(acc_empty + s, ((t >> 1) - 1) & 1, abort))) {
-                    *abort = 1;
-                    break;
+            bulk_copy_g2s(sA, p.qimg + static_cast<size_t>(qt) * a_bytes(H), a_bytes(H), a_full);
+            uint32_t issued = 0, data_tiles = 0;
+            auto load = [&](uint32_t item, bool centre) -> bool {
+                const uint32_t s = issued & 1;
+                // Stage s is free once the MMAs of load issued-2 are done (operands) and the
+                // epilogue has drained it (row data).
+                if (issued >= 2) {
+                    const uint32_t par = ((issued >> 1) - 1) & 1;
+                    if (!mbar_wait(empty + s, par, abort) || !mbar_wait(acc_empty + s, par, abort)) return false;
                 }
-                mbar_expect_tx(full + s, b_bytes(H) + kNormBytes);
-                bulk_copy_g2s(s ? sB1 : sB0, p.pimg + static_cast<size_t>(t) * b_bytes(H), b_bytes(H), full + s);
-                bulk_copy_g2s(sN + s * kTileN, p.pnorm + static_cast<size_t>(t) * kTileN, kNormBytes, full + s);
+                const uint32_t rd_bytes = (centre ? kRowData : kTileN) * sizeof(float);
+                mbar_expect_tx(full + s, b_bytes(H) + rd_bytes);
+                const uint8_t* img = centre ? p.cimg : p.pimg;
+                const float* rd = centre ? p.cdata + static_cast<size_t>(item) * kRowData
+                                         : p.pnorm + static_cast<size_t>(item) * kTileN;
+                bulk_copy_g2s(s ? sB1 : sB0, img + static_cast<size_t>(item) * b_bytes(H), b_bytes(H), full + s);
+                bulk_copy_g2s(sN + s * kRowData, rd, rd_bytes, full + s);
                 ++issued;
+                data_tiles += centre ? 0u : 1u;
+                return true;
+            };
+            bool ok = true;
+            uint32_t item;
+            bool centre;
+            for (uint32_t st = 0; ok && st < 3; ++st) {
+                if (st == 2) ok = mbar_wait(mask_ready, 0, abort) && !*abort;
+                seq.begin(st);
+                while (ok && seq.next(&item, &centre)) ok = load(item, centre);
             }
-            if (*abort) {
-                // Let copies already in flight land before the block can exit.
-                mbar_wait(a_full, 0, abort);
-                for (uint32_t t = issued >= 2 ? issued - 2 : 0; t < issued; ++t) {
-                    volatile int never = 0;
-                    mbar_wait(full + (t & 1), (t >> 1) & 1, &never);
-                }
+            if (!ok) {
+                *abort = 1;
+                // Let copies in flight land before the block can exit.
+                volatile int never = 0;
+                mbar_wait(a_full, 0, &never);
+                for (uint32_t i = issued >= 2 ? issued - 2 : 0; i < issued; ++i)
+                    mbar_wait(full + (i & 1), (i >> 1) & 1, &never);
             }
+            if (p.counters && data_tiles) atomicAdd(&p.counters->leaves, static_cast<unsigned long long>(data_tiles));
         }
     } else if (warp == 1) {
         if (lane == 0) {
             // MMA issuer.
-            constexpr uint32_t idesc = idesc_bf16(kTileM, kTileN);
-            bool ok = mbar_wait(a_full, 0, abort);
             const uint32_t a0 = smem_addr(sA);
-            for (uint32_t t = 0; ok && t < ptiles; ++t) {
-                const uint32_t s = t & 1, b = t & 1;
-                if (!mbar_wait(full + s, (t >> 1) & 1, abort)) {
-                    ok = false;
-                    break;
-                }
-                if (t >= 2 && !mbar_wait(acc_empty + b, ((t >> 1) - 1) & 1, abort)) {
-                    ok = false;
-                    break;
-                }
+            uint32_t i = 0;
+            auto mma_tile = [&]() -> bool {
+                const uint32_t s = i & 1;
+                if (!mbar_wait(full + s, (i >> 1) & 1, abort)) return false;
+                if (i >= 2 && !mbar_wait(acc_empty + s, ((i >> 1) - 1) & 1, abort)) return false;
                 tc_fence_after();
                 const uint32_t b0 = smem_addr(s ? sB1 : sB0);
-#pragma unroll
-                for (uint32_t h = 0; h < H; ++h)
-#pragma unroll
-                    for (uint32_t kk = 0; kk < 4; ++kk)
-                        mma_bf16(tmem + b * kTileN, desc_sw128(a0 + h * kTileM * 128u + kk * 32u),
-                                 desc_sw128(b0 + h * kTileN * 128u + kk * 32u), idesc, (h | kk) != 0);
+                for (uint32_t ks = 0; ks < p.ksteps; ++ks) {
+                    const uint32_t h = ks >> 2, kk = ks & 3;
+                    mma_f16kind(tmem + s * kTileN, desc_sw128(a0 + h * kTileM * 128u + kk * 32u),
+                                desc_sw128(b0 + h * kTileN * 128u + kk * 32u), p.idesc, ks != 0);
+                }
                 mma_commit(empty + s);
-                mma_commit(acc_full + b);
+                mma_commit(acc_full + s);
+                ++i;
+                return true;
+            };
+            bool ok = mbar_wait(a_full, 0, abort);
+            uint32_t item;
+            bool centre;
+            for (uint32_t st = 0; ok && st < 3; ++st) {
+                if (st == 2) ok = mbar_wait(mask_ready, 0, abort) && !*abort;
+                seq.begin(st);
+                while (ok && seq.next(&item, &centre)) ok = mma_tile();
             }
-            if (!ok) *abort = 1;
+            if (!ok) {
+                *abort = 1;
+                // The MMAs already issued finish before TMEM is released.
+                volatile int never = 0;
+                if (i) mbar_wait(acc_full + ((i - 1) & 1), ((i - 1) >> 1) & 1, &never);
+            }
         }
     } else {
         // Epilogue: thread = query row.  TMEM lanes 32*(warp%4) .. +31 belong to this warp.
         const uint32_t quarter = warp & 3;
         const uint32_t row = quarter * 32 + lane;
-        const uint32_t q = blockIdx.x * kTileM + row;  // row of the batch (position in the list)
-        const bool live = q < live_rows;
-        const uint32_t qi = live ? (p.order ? p.order[q] : q) : 0u;
-        const float2 qn = live ? p.qnorm[q] : make_float2(0.0f, 0.0f);
-        const float seed = live ? (p.radii ? fminf(p.radii[qi], p.max_d2) : p.max_d2) : 0.0f;
+        const uint32_t r = qt * kTileM + row;  // row of the sorted batch
+        const bool live = r < live_rows;
+        const uint32_t qi = live ? p.order[r] : 0u;
+        const float nq = live ? p.qnorm[r] : 0.0f;
+        const bool good = live && nq <= FLT_MAX;  // NaN or +inf: not representable
+        const Bounds& b = p.b;
+        const float r2 = fminf(p.radii ? fminf(p.radii[qi], p.max_d2) : p.max_d2, p.seed[qi]);
+        const float seed = good ? __fmul_ru(r2, p.s2) : 0.0f;
         BoundHeap heap{heap_base + row, p.k};
         for (uint32_t i = 0; i < p.k; ++i) heap.at(i) = seed;
         float T = seed;
-        const float one_m = __fsub_rd(1.0f, p.g), one_p = __fadd_ru(1.0f, p.g);
-        const float c2_hi = __fadd_ru(1.0f, p.c2);
-        const float c1q = __fmul_ru(p.c1, qn.y);
-        // Candidate test as a threshold on G:  G >= alpha |p|^2 - beta |p| + gam, all rounded down.
-        const float alpha = __fmul_rd(0.5f, 1.0f - p.c2);
-        const float beta = __fmul_ru(0.5f * p.c1, qn.y);
-        auto gamma_of = [&](float tb) {
-            const float tp = __fdiv_ru(tb, one_m);  // T / (1 - g), rounded up
-            return __fsub_rd(__fmul_rd(alpha, qn.x), __fmul_ru(0.5f, tp));
+        const float qup = good ? __fsqrt_ru(__fmul_ru(nq, __fadd_ru(1.0f, b.gn))) : 0.0f;  // >= |q'|
+        const float one_m_gn = __fsub_rd(1.0f, b.gn);
+        const float a = __fmul_rd(0.5f, one_m_gn);
+        const float a_q = __fmul_rd(a, nq);
+        const float up_n = __fadd_ru(1.0f, b.gn);
+        const float up_g = __fadd_ru(1.0f, b.g);
+        const float c1q = __fmul_ru(b.c1, qup);
+        auto bound_e = [&](float pm) { return __fadd_ru(__fmaf_ru(c1q, pm, __fmul_ru(b.c3, __fadd_ru(qup, pm))), b.c4); };
+        float E = 0.0f, theta0 = 0.0f, theta = INFINITY;
+        auto set_theta = [&]() {
+            const float tp = __fmul_ru(T, b.inv_one_m);  // >= T / (1 - g)
+            theta = good ? fmaxf(__fsub_rd(theta0, __fmul_ru(0.5f, tp)), -FLT_MAX) : INFINITY;
         };
-        float gam = gamma_of(T);
         uint32_t count = 0;
-        uint32_t* my_cand = p.cand + static_cast<size_t>(live ? q : 0) * p.cap;
+        uint32_t* my_cand = p.cand + static_cast<size_t>(live ? r : 0) * p.cap;
+        float* my_v = p.cand_v + static_cast<size_t>(live ? r : 0) * p.cap;
         const uint32_t taddr_row = tmem + ((quarter * 32u) << 16);
-        bool ok = true;
-        for (uint32_t t = 0; t < ptiles; ++t) {
-            const uint32_t b = t & 1;
+        uint32_t i = 0;
+        auto process = [&](uint32_t item, bool centre) -> bool {
+            const uint32_t s = i & 1;
             // The TMEM loads below are warp-collective: the whole warp proceeds or leaves.
-            // acc_full: the MMAs are done; full: this tile's norms landed in shared memory
-            // (already complete, waited on to observe the copy's writes).
-            const bool got = mbar_wait(acc_full + b, (t >> 1) & 1, abort) && mbar_wait(full + b, (t >> 1) & 1, abort);
-            if (!__all_sync(0xFFFFFFFFu, got)) {
-                ok = false;
-                break;
-            }
+            const bool got = mbar_wait(acc_full + s, (i >> 1) & 1, abort) && mbar_wait(full + s, (i >> 1) & 1, abort);
+            if (!__all_sync(0xFFFFFFFFu, got)) return false;
             tc_fence_after();
-            const float2* pn = sN + b * kTileN;
-            const uint32_t base = t * kTileN;
-#pragma unroll 1
-            for (uint32_t c = 0; c < kTileN / 32; ++c) {
-                float v[32];
-                tmem_ld32(taddr_row + b * kTileN + c * 32, v);
+            const float* rd = sN + s * kRowData;
+            const uint32_t tcol = taddr_row + s * kTileN;
+            // Chunks of 32 accumulator columns; the TMEM load of chunk c+1 is in flight while
+            // chunk c is processed.
+            uint32_t ra[32], rb[32];
+            tmem_ld32_async(tcol, ra);
+            tmem_wait_ld(ra);
+            if (centre) {
+                // Cell test: keep cell c when S_lo(q, c) <= (R_c + t)^2 for some query.
+                const float Ec = bound_e(__ldg(p.cmax + item));
+                const float base = __fsub_rd(__fmul_rd(one_m_gn, nq), __fmul_ru(2.0f, Ec));
+                const float t2 = __fmul_ru(__fadd_ru(T, b.c4), b.inv_one_m);
+                const float tq = __fsqrt_ru(t2);
+                const float tq2 = __fmul_ru(tq, tq);
+                const float tq_2 = __fmul_ru(2.0f, tq);
+                auto chunk = [&](const uint32_t (&r)[32], uint32_t c) {
+                    uint32_t bits = 0;
 #pragma unroll
-                for (uint32_t i = 0; i < 32; ++i) {
-                    const uint32_t jl = c * 32 + i;
-                    const float2 pp = pn[jl];
-                    const float theta = __fmaf_rd(alpha, pp.x, __fmaf_rd(-beta, pp.y, gam));
-                    if (live && v[i] >= theta && base + jl < p.n) {
-                        if (count < p.cap) my_cand[count] = base + jl;
-                        ++count;
-                        // Upper bound of this pair's float distance.
-                        const float s = __fadd_ru(qn.x, pp.x);
-                        const float hi = __fmaf_ru(-2.0f, v[i], __fmaf_ru(c1q, pp.y, __fmul_ru(c2_hi, s)));
-                        const float u = __fmul_ru(fmaxf(hi, 0.0f), one_p);
+                    for (uint32_t j = 0; j < 32; ++j) {
+                        const float cn = rd[c * 32 + j], cr = rd[kTileN + c * 32 + j];
+                        const float s_lo = __fmaf_rd(-2.0f, __uint_as_float(r[j]), __fmaf_rd(one_m_gn, cn, base));
+                        const float y = __fmaf_ru(cr, __fadd_ru(cr, tq_2), tq2);
+                        bits |= !(s_lo > y) ? (1u << j) : 0u;
+                    }
+                    bits = __reduce_or_sync(0xFFFFFFFFu, good ? bits : 0u);
+                    const uint32_t w = item * (kTileN / 32) + c;
+                    if (lane == 0 && bits && w < kMaskWords) atomicOr(sMask + w, bits);
+                };
+                // (The TMEM loads and waits are warp-collective: the warp reconverges before each.)
+#pragma unroll 1
+                for (uint32_t c = 0; c < kTileN / 32; c += 2) {
+                    tmem_ld32_async(tcol + (c + 1) * 32, rb);
+                    chunk(ra, c);
+                    __syncwarp();
+                    tmem_wait_ld(rb);
+                    if (c + 2 < kTileN / 32) tmem_ld32_async(tcol + (c + 2) * 32, ra);
+                    chunk(rb, c + 1);
+                    __syncwarp();
+                    if (c + 2 < kTileN / 32) tmem_wait_ld(ra);
+                }
+            } else {
+                E = bound_e(__ldg(p.pmax + item));
+                theta0 = __fsub_rd(a_q, E);
+                set_theta();
+                const float E2 = __fmul_ru(2.0f, E);
+                const float4* pn4 = reinterpret_cast<const float4*>(rd);
+                const uint32_t base = item * kTileN;
+                auto chunk = [&](const uint32_t (&r)[32], uint32_t c) {
+                    // The hit mask first, branch-free; then this lane's hits: recorded, and folded
+                    // into the bound heap afterwards so that lanes with hits update side by side
+                    // (theta is up to one chunk stale, which only keeps extra candidates).
+                    uint32_t m = 0;
+#pragma unroll
+                    for (uint32_t j4 = 0; j4 < 8; ++j4) {
+                        const float4 n4 = pn4[c * 8 + j4];
+                        const float nn[4] = {n4.x, n4.y, n4.z, n4.w};
+#pragma unroll
+                        for (uint32_t e = 0; e < 4; ++e)
+                            m |= (__fmaf_ru(-a, nn[e], __uint_as_float(r[j4 * 4 + e])) >= theta) ? (1u << (j4 * 4 + e)) : 0u;
+                    }
+                    if (m == 0) return;
+                    float hv[32], hn[32];
+                    uint32_t nh = 0;
+#pragma unroll
+                    for (uint32_t j = 0; j < 32; ++j) {
+                        if (m & (1u << j)) {
+                            const float vj = __uint_as_float(r[j]);
+                            if (count < p.cap) {
+                                my_cand[count] = base + c * 32 + j;
+                                my_v[count] = vj;
+                            }
+                            ++count;
+                            hv[nh] = vj;
+                            hn[nh] = rd[c * 32 + j];
+                            ++nh;
+                        }
+                    }
+                    bool moved = false;
+                    for (uint32_t x = 0; x < nh; ++x) {
+                        // Upper bound of this pair's float distance (scaled).
+                        const float hi = __fmaf_ru(-2.0f, hv[x], __fadd_ru(E2, __fmul_ru(up_n, __fadd_ru(nq, hn[x]))));
+                        const float u = __fmul_ru(fmaxf(hi, 0.0f), up_g);
                         if (u < T) {
                             heap.replace_top(u);
                             T = heap.at(0);
-                            gam = gamma_of(T);
+                            moved = true;
                         }
                     }
+                    if (moved) set_theta();
+                };
+                // (The TMEM loads and waits are warp-collective: the warp reconverges before each.)
+#pragma unroll 1
+                for (uint32_t c = 0; c < kTileN / 32; c += 2) {
+                    tmem_ld32_async(tcol + (c + 1) * 32, rb);
+                    chunk(ra, c);
+                    __syncwarp();
+                    tmem_wait_ld(rb);
+                    if (c + 2 < kTileN / 32) tmem_ld32_async(tcol + (c + 2) * 32, ra);
+                    chunk(rb, c + 1);
+                    __syncwarp();
+                    if (c + 2 < kTileN / 32) tmem_wait_ld(ra);
                 }
             }
             tc_fence_before();
-            mbar_arrive(acc_empty + b);
+            mbar_arrive(acc_empty + s);
+            ++i;
+            return true;
+        };
+        bool ok = true;
+        uint32_t item;
+        bool centre;
+        for (uint32_t st = 0; ok && st < 2; ++st) {
+            seq.begin(st);
+            while (ok && seq.next(&item, &centre)) ok = process(item, centre);
         }
         if (!ok) *abort = 1;
-        if (live) p.cand_count[q] = ok ? count : 0xFFFFFFFFu;
+        // Every epilogue thread reaches the barrier (the mask is complete after it) and arrives on
+        // mask_ready, failed or not; a failure seen here stops all roles.
+        epilogue_barrier();
+        mbar_arrive(mask_ready);
+        ok = __all_sync(0xFFFFFFFFu, *abort == 0 && mbar_wait(mask_ready, 0, abort)) && *abort == 0;
+        if (ok) {
+            seq.begin(2);
+            while (ok && seq.next(&item, &centre)) ok = process(item, centre);
+        }
+        if (!ok) *abort = 1;
+        if (live) {
+            p.cand_count[r] = (ok && good) ? count : kNone;
+            p.final_t[r] = T;
+        }
     }
     tc_fence_before();
     __syncthreads();
@@ -276,73 +516,438 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
 }
 
 // Exact rescoring: the reference's sequential FP32 distance for every candidate, top-k by key.
-// Queries whose candidate list overflowed (or whose filter block aborted) are listed for the
-// plain search instead.
-template <int PS, int KMAX>
-__global__ void __launch_bounds__(128) tc_rescore_kernel(const float* __restrict__ points, const float* __restrict__ queries,
-                                                         uint32_t dims, uint32_t nq, const uint32_t* __restrict__ cand,
-                                                         const uint32_t* __restrict__ cand_count, uint32_t cap, uint32_t k,
-                                                         float max_d2, const float* __restrict__ radii,
-                                                         const uint32_t* __restrict__ order,
-                                                         const uint32_t* __restrict__ live_count,
-                                                         int32_t* __restrict__ out_idx, float* __restrict__ out_dist,
-                                                         uint32_t* __restrict__ retry, uint32_t* __restrict__ retry_count) {
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;  // row of the batch
-    if (q >= (live_count ? *live_count : nq)) return;
-    const uint32_t qi = order ? order[q] : q;
-    const uint32_t cnt = cand_count[q];
-    if (cnt > cap) {
-        retry[atomicAdd(retry_count, 1u)] = qi;
+// A candidate is skipped, without reading its row, when its GEMM lower bound already exceeds the
+// row's final k-th upper bound T' (then its float distance exceeds the k-th one).  Rows whose
+// candidate list overflowed (or whose block gave up, or that the 16-bit format could not hold) are
+// listed for the plain search.
+struct RescoreArgs {
+    const float* pts;         // FP32 points per padded row (stride PS)
+    const uint32_t* ids;      // point index per padded row
+    const float* pnorm;       // scaled norm per padded row
+    const float* pmax;        // per point tile
+    const float* queries;
+    uint32_t dims, nq, cap, k;
+    float max_d2;
+    const float* radii;
+    const uint32_t* order;       // row -> query index
+    const uint32_t* live_count;  // rows in use (device), or null for nq
+    const uint32_t* cand;
+    const float* cand_v;
+    const uint32_t* cand_count;
+    const float* qnorm;       // per row: scaled norm of the query
+    const float* final_t;     // per row: T'
+    Bounds b;
+    int32_t* out_idx;
+    float* out_dist;
+    uint32_t* retry;
+    uint32_t* retry_count;
+    DevCounters* counters;
+};
+
+constexpr uint32_t kRescoreWarps = 4;
+constexpr uint32_t kRescoreBuf = 1024;  // keys buffered per warp before a sort-and-trim
+
+// Sorts buf[0, n) ascending (n a power of two, <= kRescoreBuf) with the lanes of one warp.
+__device__ __forceinline__ void warp_bitonic(uint64_t* buf, uint32_t n, uint32_t lane) {
+    for (uint32_t size = 2; size <= n; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t i = lane; i < n / 2; i += 32) {
+                const uint32_t lo = 2 * stride * (i / stride) + (i % stride);
+                const uint32_t hi = lo + stride;
+                const bool up = (lo & size) == 0;
+                const uint64_t x = buf[lo], y = buf[hi];
+                if ((x > y) == up) {
+                    buf[lo] = y;
+                    buf[hi] = x;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// One warp per row.  Lanes take candidates in turn; each kept candidate's exact distance is
+// computed by one lane (the reference's sequential sum over the dims), its key appended to the
+// warp's buffer; a full buffer is sorted and trimmed to the k smallest keys.
+template <int PS>
+__global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const RescoreArgs a) {
+    __shared__ uint64_t sbuf[kRescoreWarps][kRescoreBuf];
+    const uint32_t lane = threadIdx.x % 32, w = threadIdx.x / 32;
+    const uint32_t r = blockIdx.x * kRescoreWarps + w;  // row of the sorted batch
+    if (r >= (a.live_count ? *a.live_count : a.nq)) return;  // warp-uniform
+    uint64_t* buf = sbuf[w];
+    const uint32_t qi = a.order[r];
+    const uint32_t cnt = a.cand_count[r];
+    if (cnt > a.cap) {
+        if (lane == 0) {
+            a.retry[atomicAdd(a.retry_count, 1u)] = qi;
+            if (a.counters) atomicAdd(&a.counters->fallback, 1ull);
+        }
         return;
     }
     float qv[PS];
 #pragma unroll
-    for (int d = 0; d < PS; ++d) qv[d] = static_cast<uint32_t>(d) < dims ? queries[static_cast<size_t>(qi) * dims + d] : 0.0f;
-    Tracker<KMAX, false, false> tr;
-    tr.init(k, radii ? fminf(radii[qi], max_d2) : max_d2, nullptr, 0);
-    const uint32_t* c = cand + static_cast<size_t>(q) * cap;
-    for (uint32_t i = 0; i < cnt; ++i) {
-        const uint32_t j = c[i];
-        const float d2 = dist2_vec4<PS>(qv, reinterpret_cast<const float4*>(points + static_cast<size_t>(j) * PS));
-        tr.offer(make_key(d2, static_cast<int32_t>(j)));
+    for (int d = 0; d < PS; ++d) qv[d] = static_cast<uint32_t>(d) < a.dims ? a.queries[static_cast<size_t>(qi) * a.dims + d] : 0.0f;
+    const float r2 = a.radii ? fminf(a.radii[qi], a.max_d2) : a.max_d2;
+    const uint64_t limit = make_key(r2, -1);  // the key an unfilled slot holds
+    const Bounds& b = a.b;
+    const float nq = a.qnorm[r];
+    const float qup = __fsqrt_ru(__fmul_ru(nq, __fadd_ru(1.0f, b.gn)));
+    const float one_m_gn = __fsub_rd(1.0f, b.gn);
+    const float one_m_g = __fsub_rd(1.0f, b.g);
+    const float c1q = __fmul_ru(b.c1, qup);
+    const float tfin = a.final_t[r];
+    const uint32_t* c = a.cand + static_cast<size_t>(r) * a.cap;
+    const float* cv = a.cand_v + static_cast<size_t>(r) * a.cap;
+    uint32_t m = 0, scored = 0;
+    for (uint32_t i0 = 0; i0 < cnt; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        uint64_t key = ~0ull;
+        if (i < cnt) {
+            const uint32_t pos = c[i];
+            const float pm = __ldg(a.pmax + pos / kTileN);
+            const float E = __fadd_ru(__fmaf_ru(c1q, pm, __fmul_ru(b.c3, __fadd_ru(qup, pm))), b.c4);
+            // Lower bound of s^2 times the pair's float distance.
+            const float lo = __fsub_rd(__fmaf_rd(-2.0f, cv[i], __fmul_rd(one_m_gn, __fadd_rd(nq, __ldg(a.pnorm + pos)))),
+                                       __fmul_ru(2.0f, E));
+            if (!(__fmul_rd(__fsub_rd(lo, b.c4), one_m_g) > tfin)) {
+                ++scored;
+                const float d2 = dist2_vec4<PS>(qv, reinterpret_cast<const float4*>(a.pts + static_cast<size_t>(pos) * PS));
+                key = make_key(d2, static_cast<int32_t>(a.ids[pos]));
+            }
+        }
+        const bool take = key < limit;
+        const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, take);
+        if (m + 32 > kRescoreBuf) {
+            // Sort and keep the k smallest (the rest cannot be in the answer).
+            uint32_t n2 = 1;
+            while (n2 < m) n2 <<= 1;
+            for (uint32_t j = m + lane; j < n2; j += 32) buf[j] = ~0ull;
+            __syncwarp();
+            warp_bitonic(buf, n2, lane);
+            m = min(m, a.k);
+        }
+        if (take) buf[m + __popc(ballot & ((1u << lane) - 1u))] = key;
+        m += __popc(ballot);
+        __syncwarp();
     }
-    tr.emit(k, out_idx + static_cast<size_t>(qi) * k, out_dist + static_cast<size_t>(qi) * k);
+    uint32_t n2 = 1;
+    while (n2 < m) n2 <<= 1;
+    for (uint32_t j = m + lane; j < n2; j += 32) buf[j] = ~0ull;
+    __syncwarp();
+    if (m > 1) warp_bitonic(buf, n2, lane);
+    for (uint32_t j = lane; j < a.k; j += 32) {
+        const uint64_t key = j < m ? buf[j] : limit;
+        a.out_idx[static_cast<size_t>(qi) * a.k + j] = j < m ? key_index(key) : -1;
+        a.out_dist[static_cast<size_t>(qi) * a.k + j] = j < m ? key_dist(key) : r2;
+    }
+    if (a.counters) {
+        for (int o = 16; o; o >>= 1) scored += __shfl_xor_sync(0xFFFFFFFFu, scored, o);
+        if (lane == 0) atomicAdd(&a.counters->nodes, static_cast<unsigned long long>(scored));
+    }
 }
 
-// Packs rows of float data ([rows][dims]) into the 128-byte-swizzle BF16 image of `tile`-row
-// tiles with H 64-element halves, and writes {sum x^2, sqrt} per row.  Rows past `rows` and
-// columns past `dims` are zero.
-__global__ void tc_pack_kernel(const float* __restrict__ src, uint32_t rows, uint32_t dims, uint32_t src_stride,
-                               uint32_t tile, uint32_t H, uint8_t* __restrict__ img, float2* __restrict__ norms,
-                               uint32_t padded_rows, const uint32_t* __restrict__ order = nullptr,
-                               const uint32_t* __restrict__ live_count = nullptr) {
+// One thread per padded row: gathers source row row_of[r] (identity when row_of is null; rows
+// past the live count or mapped to kNone are padding), scales it by `scale`, rounds it to FP16 or
+// BF16 into the 128-byte-swizzle image of `tile_rows`-row tiles with H 64-element halves, and
+// writes the float norm of the scaled row (padding: pad_norm; not representable: NaN, and
+// *bad is set).  Optionally keeps an unscaled FP32 copy (zero padded) and the row's point index.
+__global__ void tc_pack_kernel(const float* __restrict__ src, uint32_t src_stride, uint32_t dims,
+                               const uint32_t* __restrict__ row_of, uint32_t rows, const uint32_t* __restrict__ live_count,
+                               uint32_t tile_rows, uint32_t H, bool f16, float scale, uint8_t* __restrict__ img,
+                               float* __restrict__ norm, float pad_norm, float* __restrict__ copy, uint32_t copy_stride,
+                               const uint32_t* __restrict__ src_ids, uint32_t* __restrict__ ids, uint32_t padded_rows,
+                               int* __restrict__ bad) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= padded_rows) return;
-    const uint32_t t = r / tile, rr = r % tile;
-    uint8_t* base = img + static_cast<size_t>(t) * H * tile * 128u;
-    const bool valid = r < (live_count ? *live_count : rows);
-    const uint32_t sr = valid ? (order ? order[r] : r) : 0u;  // source row
+    const uint32_t t = r / tile_rows, rr = r % tile_rows;
+    uint8_t* base = img + static_cast<size_t>(t) * H * tile_rows * 128u;
+    const bool live = r < (live_count ? *live_count : rows);
+    const uint32_t sr = live ? (row_of ? row_of[r] : r) : kNone;
+    const bool valid = sr != kNone;
     float acc = 0.0f;
+    bool inf = false;
     for (uint32_t k = 0; k < 64 * H; ++k) {
         const float x = (valid && k < dims) ? src[static_cast<size_t>(sr) * src_stride + k] : 0.0f;
-        acc = __fmaf_rn(x, x, acc);
-        const __nv_bfloat16 b = __float2bfloat16_rn(x);
-        *reinterpret_cast<__nv_bfloat16*>(base + sw128_offset(tile, rr, k)) = b;
+        const float xs = x * scale;  // exact: scale is a power of two and the result stays finite
+        acc = __fmaf_rn(xs, xs, acc);
+        uint16_t bits;
+        if (f16) {
+            const __half h = __float2half_rn(xs);
+            inf |= __hisinf(h) != 0 || __hisnan(h);
+            bits = __half_as_ushort(h);
+        } else {
+            const __nv_bfloat16 h = __float2bfloat16_rn(xs);
+            const float back = __bfloat162float(h);
+            inf |= !(fabsf(back) <= FLT_MAX);
+            bits = __bfloat16_as_ushort(h);
+        }
+        *reinterpret_cast<uint16_t*>(base + sw128_offset(tile_rows, rr, k)) = bits;
+        if (copy && k < copy_stride) copy[static_cast<size_t>(r) * copy_stride + k] = x;
     }
-    norms[r] = make_float2(acc, sqrtf(acc));
+    const bool ok = !inf && acc <= FLT_MAX;
+    norm[r] = valid ? (ok ? acc : __int_as_float(0x7fc00000)) : pad_norm;
+    if (valid && !ok && bad) atomicExch(bad, 1);
+    if (ids) ids[r] = valid ? (src_ids ? src_ids[sr] : sr) : kNone;
+}
+
+// Nearest landmark (float distance, lowest index on ties) of each row; rows past the live count
+// get key `cells`.  keys/vals are indexed by row; vals = the source row.  With `cell_far` (per
+// cell: float squared distance from the landmark to its farthest point) and `cell_start`, also
+// writes seed[source row]: an upper bound on the float distance from the row to its k-th
+// nearest point, (|x - l| + r)^2 over the landmark's own cell when that holds >= k points, else
+// +inf (rounded up, margins g for the float distances and 2^-120 for subnormal ones).
+template <int DP>
+__global__ void __launch_bounds__(128) tc_assign_kernel(const float* __restrict__ src, uint32_t stride, uint32_t dims,
+                                                        uint32_t rows, const uint32_t* __restrict__ order,
+                                                        const uint32_t* __restrict__ live_count,
+                                                        const float* __restrict__ land, uint32_t ps, uint32_t cells,
+                                                        uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                        const float* __restrict__ cell_far,
+                                                        const uint32_t* __restrict__ cell_start, uint32_t k,
+                                                        float* __restrict__ seed) {
+    constexpr uint32_t kChunk = 64;
+    __shared__ float sl[kChunk * DP];
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = r < rows && r < (live_count ? *live_count : rows);
+    const uint32_t row = live ? (order ? order[r] : r) : 0u;
+    float q[DP];
+#pragma unroll
+    for (int d = 0; d < DP; ++d) q[d] = (live && static_cast<uint32_t>(d) < dims) ? src[static_cast<size_t>(row) * stride + d] : 0.0f;
+    float best = INFINITY;
+    uint32_t bi = 0;
+    for (uint32_t c0 = 0; c0 < cells; c0 += kChunk) {
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < kChunk * DP; e += blockDim.x) {
+            const uint32_t j = e / DP, d = e % DP;
+            sl[e] = c0 + j < cells ? land[static_cast<size_t>(c0 + j) * ps + d] : 0.0f;
+        }
+        __syncthreads();
+        const uint32_t jn = min(kChunk, cells - c0);
+        for (uint32_t j = 0; j < jn; ++j) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int d = 0; d < DP; ++d) {
+                const float t = __fsub_rn(q[d], sl[j * DP + d]);
+                acc = __fmaf_rn(t, t, acc);
+            }
+            if (acc < best) {
+                best = acc;
+                bi = c0 + j;
+            }
+        }
+    }
+    if (r < rows) {
+        keys[r] = live ? bi : cells;
+        vals[r] = row;
+        if (seed && live) {
+            float t = INFINITY;
+            if (best <= FLT_MAX && cell_start[bi + 1] - cell_start[bi] >= k) {
+                const float g = rel_margin(dims);
+                const float inv = __frcp_ru(__fsub_rd(1.0f, g));  // >= 1 / (1 - g)
+                const float a = __fsqrt_ru(__fmul_ru(best, inv));  // >= exact |x - l|
+                const float b = __fsqrt_ru(__fmul_ru(cell_far[bi], inv));
+                // Plus 2^-120 for float distances whose terms fall in the subnormal range.
+                t = __fadd_ru(__fmul_ru(__fmul_ru(__fadd_ru(a, b), __fadd_ru(a, b)), __fadd_ru(1.0f, g)), 0x1p-120f);
+            }
+            seed[row] = t;
+        }
+    }
+}
+
+// Farthest row of each cell from its landmark, as (distance bits << 32) | row.
+__global__ void tc_cell_far_kernel(const float* __restrict__ src, uint32_t stride, uint32_t dims,
+                                   const uint32_t* __restrict__ cell, uint32_t rows, const float* __restrict__ land,
+                                   uint32_t ps, unsigned long long* __restrict__ far) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const uint32_t c = cell[r];
+    const float* x = src + static_cast<size_t>(r) * stride;
+    const float* l = land + static_cast<size_t>(c) * ps;
+    float acc = 0.0f;
+    for (uint32_t d = 0; d < dims; ++d) {
+        const float t = __fsub_rn(x[d], l[d]);
+        acc = __fmaf_rn(t, t, acc);
+    }
+    atomicMax(far + c, (static_cast<unsigned long long>(__float_as_uint(acc)) << 32) | r);
+}
+
+// Padded position of each sorted point row: cell c's rows fill tiles cell_tile[c].. in order.
+__global__ void tc_place_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n,
+                                const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ cell_tile,
+                                uint32_t* __restrict__ row_of) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t c = keys[i];
+    row_of[static_cast<size_t>(cell_tile[c]) * kTileN + (i - cell_start[c])] = vals[i];
+}
+
+// Home range of each query tile: the cells of its (cell-sorted) queries, widened by whole
+// neighbouring cells until they hold at least `min_points` points; written as first tile, end
+// tile, first cell, last cell.
+__global__ void tc_home_kernel(const uint32_t* __restrict__ cell_sorted, const uint32_t* __restrict__ live_count,
+                               uint32_t nq, const uint32_t* __restrict__ cell_start,
+                               const uint32_t* __restrict__ cell_tile, uint32_t cells, uint32_t min_points,
+                               uint32_t qtiles, uint32_t* __restrict__ home) {
+    const uint32_t qt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qt >= qtiles) return;
+    const uint32_t live = live_count ? *live_count : nq;
+    const uint32_t first = qt * kTileM;
+    if (first >= live) {
+        home[4 * qt] = home[4 * qt + 1] = home[4 * qt + 2] = home[4 * qt + 3] = 0;
+        return;
+    }
+    const uint32_t last = min(first + kTileM - 1, live - 1);
+    uint32_t c0 = min(cell_sorted[first], cells - 1), c1 = min(cell_sorted[last], cells - 1);
+    while (cell_start[c1 + 1] - cell_start[c0] < min_points && (c0 > 0 || c1 + 1 < cells)) {
+        if (c0 > 0) --c0;
+        if (c1 + 1 < cells && cell_start[c1 + 1] - cell_start[c0] < min_points) ++c1;
+    }
+    home[4 * qt] = cell_tile[c0];
+    home[4 * qt + 1] = cell_tile[c1 + 1];
+    home[4 * qt + 2] = c0;
+    home[4 * qt + 3] = c1;
+}
+
+// One warp per cell, over its padded rows (valid: finite norm), in scaled coordinates (x * scale,
+// exact): centre = the mean of its rows; radius = an upper bound on the exact distance from the
+// centre to each of them (relative margin for normal-range rounding plus 2^-64 for subnormal
+// rounding).
+__global__ void tc_cell_ball_kernel(const float* __restrict__ pts, uint32_t ps, uint32_t dims, float scale,
+                                    const float* __restrict__ norm, const uint32_t* __restrict__ cell_tile,
+                                    uint32_t cells, float margin, float* __restrict__ centre,
+                                    float* __restrict__ radius) {
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x % 32;
+    if (c >= cells) return;
+    const uint32_t r0 = cell_tile[c] * kTileN, r1 = cell_tile[c + 1] * kTileN;
+    float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    uint32_t cnt = 0;
+    for (uint32_t r = r0; r < r1; ++r) {
+        if (!(norm[r] <= FLT_MAX)) continue;
+        ++cnt;
+#pragma unroll
+        for (uint32_t m = 0; m < 4; ++m) {
+            const uint32_t d = lane + 32 * m;
+            if (d < dims) sum[m] += pts[static_cast<size_t>(r) * ps + d] * scale;
+        }
+    }
+    float cc[4];
+#pragma unroll
+    for (uint32_t m = 0; m < 4; ++m) {
+        const uint32_t d = lane + 32 * m;
+        cc[m] = (cnt && d < dims) ? sum[m] / static_cast<float>(cnt) : 0.0f;
+        if (d < ps) centre[static_cast<size_t>(c) * ps + d] = cc[m];
+    }
+    float far = 0.0f;
+    for (uint32_t r = r0; r < r1; ++r) {
+        if (!(norm[r] <= FLT_MAX)) continue;
+        float part = 0.0f;
+#pragma unroll
+        for (uint32_t m = 0; m < 4; ++m) {
+            const uint32_t d = lane + 32 * m;
+            if (d < dims) {
+                const float e = __fsub_rn(cc[m], pts[static_cast<size_t>(r) * ps + d] * scale);
+                part = __fmaf_rn(e, e, part);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
+        far = fmaxf(far, part);
+    }
+    if (lane == 0) radius[c] = cnt ? __fadd_ru(ball_radius(far, margin), 0x1p-64f) : 0.0f;
+}
+
+// Per tile of 256 rows: an upper bound on the norms of its rows (finite entries only).
+__global__ void tc_tile_max_kernel(const float* __restrict__ norm, uint32_t tiles, float gn, float* __restrict__ out) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tiles) return;
+    float m = 0.0f;
+    for (uint32_t r = 0; r < kTileN; ++r) {
+        const float v = norm[static_cast<size_t>(t) * kTileN + r];
+        if (v <= FLT_MAX) m = fmaxf(m, v);
+    }
+    out[t] = __fsqrt_ru(__fmul_ru(m, __fadd_ru(1.0f, gn)));
+}
+
+// Row data of the centre tiles: 256 norms then 256 radii per tile.
+__global__ void tc_cdata_kernel(const float* __restrict__ cnorm, const float* __restrict__ radius, uint32_t cells,
+                                uint32_t ctiles, float* __restrict__ cdata) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ctiles * kTileN) return;
+    const uint32_t t = i / kTileN, j = i % kTileN;
+    cdata[static_cast<size_t>(t) * kRowData + j] = i < cells ? cnorm[i] : INFINITY;
+    cdata[static_cast<size_t>(t) * kRowData + kTileN + j] = i < cells ? radius[i] : 0.0f;
+}
+
+// Squared float distances between all pairs of landmarks ([cells][cells]).
+__global__ void tc_pair_d2_kernel(const float* __restrict__ land, uint32_t ps, uint32_t dims, uint32_t cells,
+                                  float* __restrict__ out) {
+    const uint64_t e = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    if (e >= static_cast<uint64_t>(cells) * cells) return;
+    const float* a = land + (e / cells) * ps;
+    const float* b = land + (e % cells) * ps;
+    float acc = 0.0f;
+    for (uint32_t d = 0; d < dims; ++d) {
+        const float t = __fsub_rn(a[d], b[d]);
+        acc = __fmaf_rn(t, t, acc);
+    }
+    out[e] = acc;
+}
+
+// out[j][0..ps) = src row rows[j], zero padded past `dims`.
+__global__ void tc_gather_rows_kernel(const float* __restrict__ src, uint32_t stride, uint32_t dims,
+                                      const uint32_t* __restrict__ rows, uint32_t count, uint32_t ps,
+                                      float* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count * ps) return;
+    const uint32_t j = i / ps, d = i % ps;
+    out[i] = d < dims ? src[static_cast<size_t>(rows[j]) * stride + d] : 0.0f;
+}
+
+// Largest |coordinate| over the rows (as float bits; NaN compares largest).
+__global__ void tc_absmax_kernel(const float* __restrict__ src, uint32_t stride, uint32_t dims, uint32_t rows,
+                                 uint32_t* __restrict__ out) {
+    uint32_t m = 0;
+    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < static_cast<size_t>(rows) * dims;
+         e += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const size_t r = e / dims, d = e % dims;
+        m = max(m, __float_as_uint(src[r * stride + d]) & 0x7FFFFFFFu);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+    if (threadIdx.x % 32 == 0) atomicMax(out, m);
+}
+
+// Dense copy of a tree's occupied leaf slots (slot order): coordinates (zero padded to ps) and ids.
+__global__ void tc_gather_slots_kernel(const float* __restrict__ leaf, uint32_t leaf_stride, uint32_t id_at,
+                                       const uint32_t* __restrict__ slots, uint32_t n, uint32_t dims, uint32_t ps,
+                                       float* __restrict__ dense, uint32_t* __restrict__ ids) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* s = leaf + static_cast<size_t>(slots[i]) * leaf_stride;
+    for (uint32_t d = 0; d < ps; ++d) dense[static_cast<size_t>(i) * ps + d] = d < dims ? s[d] : 0.0f;
+    ids[i] = static_cast<uint32_t>(__float_as_int(s[id_at]));
+}
+
+__global__ void tc_slot_keys_kernel(const float* __restrict__ leaf, uint32_t leaf_stride, uint32_t id_at, uint32_t slots,
+                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= slots) return;
+    keys[i] = __float_as_int(leaf[static_cast<size_t>(i) * leaf_stride + id_at]) >= 0 ? 0u : 1u;
+    vals[i] = i;
 }
 
 // Self-test: one 128 x 256 x (64 H) tile through the same descriptors, written to global.
 template <uint32_t H>
 __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __restrict__ qimg,
-                                                             const uint8_t* __restrict__ pimg, float* __restrict__ out,
-                                                             int* __restrict__ error) {
+                                                             const uint8_t* __restrict__ pimg, uint32_t idesc,
+                                                             float* __restrict__ out, int* __restrict__ error) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = smem_addr(smem_raw);
     uint8_t* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
     uint8_t* sA = smem;
-    uint8_t* sB = sA + H * kTileM * 128u;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sB + H * kTileN * 128u);
+    uint8_t* sB = sA + a_bytes(H);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sB + b_bytes(H));
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -363,11 +968,10 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
         bulk_copy_g2s(sB, pimg, b_bytes(H), bar);
         if (mbar_wait(bar, 0, abort)) {
             tc_fence_after();
-            constexpr uint32_t idesc = idesc_bf16(kTileM, kTileN);
             for (uint32_t h = 0; h < H; ++h)
                 for (uint32_t kk = 0; kk < 4; ++kk)
-                    mma_bf16(tmem, desc_sw128(smem_addr(sA) + h * kTileM * 128u + kk * 32u),
-                             desc_sw128(smem_addr(sB) + h * kTileN * 128u + kk * 32u), idesc, (h | kk) != 0);
+                    mma_f16kind(tmem, desc_sw128(smem_addr(sA) + h * kTileM * 128u + kk * 32u),
+                                desc_sw128(smem_addr(sB) + h * kTileN * 128u + kk * 32u), idesc, (h | kk) != 0);
             mma_commit(bar + 1);
         } else {
             *abort = 1;
@@ -394,8 +998,8 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
 }
 
 size_t filter_smem(uint32_t H, uint32_t k) {
-    return 1024 + H * kTileM * 128u + 2 * H * kTileN * 128u + 2 * kTileN * sizeof(float2) +
-           static_cast<size_t>(k) * kTileM * 4 + 16 * 8;
+    return 1024 + a_bytes(H) + 2 * b_bytes(H) + 2 * kRowData * sizeof(float) + kMaskWords * sizeof(uint32_t) +
+           static_cast<size_t>(k) * kTileM * 4 + 10 * 8 + 8;
 }
 
 // The filter allocates all 512 TMEM columns, so a second resident block on the same SM would
@@ -403,92 +1007,399 @@ size_t filter_smem(uint32_t H, uint32_t k) {
 // per SM.
 size_t filter_launch_smem(uint32_t H, uint32_t k) { return std::max<size_t>(filter_smem(H, k), 120 * 1024); }
 
-}  // namespace
+uint32_t halves(uint32_t dims) { return dims <= 64 ? 1u : 2u; }
 
-bool tc_supported(uint32_t dims, uint32_t k) { return dims >= 1 && dims <= 128 && k <= 128 && filter_smem(dims <= 64 ? 1 : 2, k) <= 232448; }
+Bounds make_bounds(uint32_t dims, bool f16, float scale) {
+    const double u = f16 ? std::ldexp(1.0, -11) : std::ldexp(1.0, -8);
+    const double delta = f16 ? std::ldexp(1.0, -14) : std::ldexp(1.0, -100);
+    const double D = dims;
+    Bounds b{};
+    b.c1 = static_cast<float>((2 * u + u * u + D * std::ldexp(1.0, -20) * (1 + u) * (1 + u)) * (1 + std::ldexp(1.0, -10)));
+    b.c3 = static_cast<float>(1.01 * delta * (1 + u) * std::sqrt(D));
+    // Plus the float distance's absolute error when its terms fall in the subnormal range,
+    // (D + 4) 2^-149 unscaled, twice over, in scaled units.
+    const double s2 = static_cast<double>(scale) * scale;
+    b.c4 = static_cast<float>(1.01 * D * delta * delta + 2.0 * s2 * (D + 4) * std::ldexp(1.0, -149));
+    b.gn = rel_margin(dims);
+    b.g = rel_margin(dims);
+    float inv = static_cast<float>(1.0 / (1.0 - static_cast<double>(b.g)));
+    if (static_cast<double>(inv) < 1.0 / (1.0 - static_cast<double>(b.g))) inv = std::nextafter(inv, INFINITY);
+    b.inv_one_m = inv;
+    return b;
+}
 
-// Prepares the BF16 point image and norms of a brute-force index (once).
-int tc_prepare(knn_index* ix, cudaStream_t s) {
-    if (ix->tc_ready) return KNN_OK;
-    const uint32_t H = ix->dims <= 64 ? 1 : 2;
-    const uint32_t ptiles = ceil_div(ix->n, kTileN);
-    const uint32_t prows = ptiles * kTileN;
-    KNN_TRY(ix->tc_img.alloc(static_cast<size_t>(ptiles) * H * kTileN * 128u));
-    KNN_TRY(ix->tc_norm.alloc(static_cast<size_t>(prows) * sizeof(float2)));
-    tc_pack_kernel<<<ceil_div(prows, 128), 128, 0, s>>>(ix->points.as<float>(), ix->n, ix->dims, ix->point_stride,
-                                                        kTileN, H, ix->tc_img.as<uint8_t>(), ix->tc_norm.as<float2>(),
-                                                        prows);
+int launch_assign(uint32_t dp, const float* src, uint32_t stride, uint32_t dims, uint32_t rows, const uint32_t* order,
+                  const uint32_t* live_count, const float* land, uint32_t ps, uint32_t cells, uint32_t* keys,
+                  uint32_t* vals, cudaStream_t s, const float* cell_far = nullptr, const uint32_t* cell_start = nullptr,
+                  uint32_t k = 0, float* seed = nullptr) {
+    const uint32_t grid = ceil_div(rows, 128);
+#define KNN_ASSIGN(D_)                                                                                         \
+    case D_:                                                                                                   \
+        tc_assign_kernel<D_><<<grid, 128, 0, s>>>(src, stride, dims, rows, order, live_count, land, ps, cells, \
+                                                   keys, vals, cell_far, cell_start, k, seed);                 \
+        break;
+    switch (dp) {
+        KNN_ASSIGN(1) KNN_ASSIGN(2) KNN_ASSIGN(3) KNN_ASSIGN(4) KNN_ASSIGN(8) KNN_ASSIGN(16) KNN_ASSIGN(32)
+        KNN_ASSIGN(64) KNN_ASSIGN(128)
+        default: return fail(KNN_ERR_UNSUPPORTED, "dims");
+    }
+#undef KNN_ASSIGN
     KNN_LAUNCHED();
-    ix->tc_ready = true;
-    ix->device_bytes += ix->tc_img.bytes + ix->tc_norm.bytes;
     return KNN_OK;
 }
 
-template <int PS, int KMAX>
-static int rescore(knn_index* ix, const QueryArgs& a, const uint32_t* cand, const uint32_t* cnt, uint32_t cap,
-                   uint32_t* retry, uint32_t* retry_count, cudaStream_t s) {
-    tc_rescore_kernel<PS, KMAX><<<ceil_div(a.count, 128), 128, 0, s>>>(
-        ix->points.as<float>(), a.queries, ix->dims, a.count, cand, cnt, cap, a.k, a.max_d2, a.radii, a.order,
-        a.count_dev, a.out_idx, a.out_dist, retry, retry_count);
+}  // namespace
+
+bool tc_supported(uint32_t dims, uint32_t k) {
+    return dims >= 1 && dims <= kMaxDims && k >= 1 && k <= kMaxK && filter_smem(halves(dims), k) <= 232448;
+}
+
+// Builds the cells, operand images, norms, FP32 copy, ids and cell balls of an index (once).
+int tc_prepare(knn_index* ix, cudaStream_t s) {
+    auto& T = ix->tc;
+    if (T.ready) return T.usable ? KNN_OK : fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: coordinates out of range");
+    const uint32_t n = ix->n, dims = ix->dims, ps = round_up4(ix->dp), H = halves(dims);
+    // Dense source rows: the brute-force points, or a tree's occupied leaf slots in slot order.
+    DevBuf dense_buf;
+    const float* src = nullptr;
+    uint32_t stride = 0;
+    const uint32_t* src_ids = nullptr;
+    if (ix->structure == KNN_BRUTE_FORCE) {
+        src = ix->points.as<float>();
+        stride = ix->point_stride;
+    } else {
+        const uint32_t slots = (1u << ix->node_depth) * ix->leaf_slots;
+        DevBuf tmp;
+        KNN_TRY(tmp.alloc(carve_bytes({slots * 4ull, slots * 4ull, slots * 4ull, slots * 4ull, radix_sort_temp_bytes(slots)})));
+        Carver c(tmp.ptr);
+        uint32_t* k0 = c.take<uint32_t>(slots);
+        uint32_t* v0 = c.take<uint32_t>(slots);
+        uint32_t* k1 = c.take<uint32_t>(slots);
+        uint32_t* v1 = c.take<uint32_t>(slots);
+        void* st = c.take<uint8_t>(radix_sort_temp_bytes(slots));
+        tc_slot_keys_kernel<<<ceil_div(slots, 256), 256, 0, s>>>(ix->leaf.as<float>(), ix->leaf_stride, ix->leaf_id_at,
+                                                                 slots, k0, v0);
+        KNN_LAUNCHED();
+        bool alt = false;
+        KNN_TRY(radix_sort_pairs(k0, v0, k1, v1, slots, 1, st, s, &alt));
+        KNN_TRY(dense_buf.alloc(carve_bytes({static_cast<size_t>(n) * ps * 4, n * 4ull})));
+        Carver dc(dense_buf.ptr);
+        float* dense = dc.take<float>(static_cast<size_t>(n) * ps);
+        uint32_t* ids = dc.take<uint32_t>(n);
+        tc_gather_slots_kernel<<<ceil_div(n, 128), 128, 0, s>>>(ix->leaf.as<float>(), ix->leaf_stride, ix->leaf_id_at,
+                                                                alt ? v1 : v0, n, dims, ps, dense, ids);
+        KNN_LAUNCHED();
+        KNN_TRY_CUDA(cudaStreamSynchronize(s));
+        src = dense;
+        stride = ps;
+        src_ids = ids;
+    }
+
+    // Scale: largest |coordinate| * 2^e in [2^13, 2^14) with e >= 0, else BF16.
+    DevBuf small;
+    KNN_TRY(small.alloc(256));
+    KNN_TRY_CUDA(cudaMemsetAsync(small.ptr, 0, 256, s));
+    const uint32_t am_grid = static_cast<uint32_t>(
+        std::max<uint64_t>(1, std::min<uint64_t>((static_cast<uint64_t>(n) * dims + 255) / 256, 4ull * sm_count())));
+    tc_absmax_kernel<<<am_grid, 256, 0, s>>>(src, stride, dims, n, small.as<uint32_t>());
     KNN_LAUNCHED();
+    uint32_t mbits = 0;
+    KNN_TRY_CUDA(cudaMemcpyAsync(&mbits, small.ptr, 4, cudaMemcpyDeviceToHost, s));
+    KNN_TRY_CUDA(cudaStreamSynchronize(s));
+    float M;
+    std::memcpy(&M, &mbits, 4);
+    T.ready = true;
+    T.usable = false;
+    if (!(M <= FLT_MAX)) return fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: non-finite coordinates");
+    T.f16 = M <= 16384.0f;
+    int e = 0;
+    if (T.f16 && M > 0.0f)
+        while (e < 60 && std::ldexp(static_cast<double>(M), e + 1) < 16384.0) ++e;
+    T.scale = T.f16 ? std::ldexp(1.0f, e) : 1.0f;
+    T.ps = ps;
+
+    // Landmarks: every (n/L)-th point; then, up to three times, a landmark at the farthest point
+    // of each cell whose farthest squared distance exceeds 4x the 25th percentile over cells (a
+    // cell holding two clusters is split); finally the landmarks in the order of a greedy
+    // nearest-neighbour chain, so that consecutive cells lie near each other.
+    std::vector<uint32_t> lrows;
+    {
+        const uint32_t L0 = std::max(1u, std::min(kMaxCells / 2, n / kCellPoints));
+        for (uint32_t j = 0; j < L0; ++j) lrows.push_back(static_cast<uint32_t>(static_cast<uint64_t>(j) * n / L0));
+    }
+    DevBuf sortb;
+    KNN_TRY(sortb.alloc(carve_bytes({n * 4ull, n * 4ull, n * 4ull, n * 4ull, radix_sort_temp_bytes(n), kMaxCells * 8ull,
+                                     kMaxCells * 4ull})));
+    Carver sc(sortb.ptr);
+    uint32_t* k0 = sc.take<uint32_t>(n);
+    uint32_t* v0 = sc.take<uint32_t>(n);
+    uint32_t* k1 = sc.take<uint32_t>(n);
+    uint32_t* v1 = sc.take<uint32_t>(n);
+    void* st = sc.take<uint8_t>(radix_sort_temp_bytes(n));
+    unsigned long long* far = sc.take<unsigned long long>(kMaxCells);
+    uint32_t* lr = sc.take<uint32_t>(kMaxCells);
+    KNN_TRY(T.land.alloc(static_cast<size_t>(kMaxCells) * ps * 4));
+    auto place_landmarks = [&]() -> int {
+        const uint32_t cells = static_cast<uint32_t>(lrows.size());
+        KNN_TRY_CUDA(cudaMemcpyAsync(lr, lrows.data(), cells * 4ull, cudaMemcpyHostToDevice, s));
+        tc_gather_rows_kernel<<<ceil_div(cells * ps, 256), 256, 0, s>>>(src, stride, dims, lr, cells, ps,
+                                                                       T.land.as<float>());
+        KNN_LAUNCHED();
+        KNN_TRY(launch_assign(ix->dp, src, stride, dims, n, nullptr, nullptr, T.land.as<float>(), ps, cells, k0, v0, s));
+        KNN_TRY_CUDA(cudaStreamSynchronize(s));  // lrows is reused
+        return KNN_OK;
+    };
+    for (int round = 0;; ++round) {
+        const uint32_t cells = static_cast<uint32_t>(lrows.size());
+        KNN_TRY(place_landmarks());
+        if (round == 3 || cells >= kMaxCells) break;
+        KNN_TRY_CUDA(cudaMemsetAsync(far, 0, cells * 8ull, s));
+        tc_cell_far_kernel<<<ceil_div(n, 256), 256, 0, s>>>(src, stride, dims, k0, n, T.land.as<float>(), ps, far);
+        KNN_LAUNCHED();
+        std::vector<unsigned long long> hfar(cells);
+        KNN_TRY_CUDA(cudaMemcpyAsync(hfar.data(), far, cells * 8ull, cudaMemcpyDeviceToHost, s));
+        KNN_TRY_CUDA(cudaStreamSynchronize(s));
+        std::vector<float> d2;
+        for (auto f : hfar) {
+            float v;
+            const uint32_t bits = static_cast<uint32_t>(f >> 32);
+            std::memcpy(&v, &bits, 4);
+            if (f) d2.push_back(v);
+        }
+        if (d2.empty()) break;
+        std::vector<float> sorted = d2;
+        std::nth_element(sorted.begin(), sorted.begin() + sorted.size() / 4, sorted.end());
+        const float q25 = sorted[sorted.size() / 4];
+        uint32_t added = 0;
+        for (uint32_t c = 0; c < cells && lrows.size() < kMaxCells; ++c) {
+            if (!hfar[c]) continue;
+            float v;
+            const uint32_t bits = static_cast<uint32_t>(hfar[c] >> 32);
+            std::memcpy(&v, &bits, 4);
+            if (v > 4.0f * q25 && v > 0.0f) {
+                lrows.push_back(static_cast<uint32_t>(hfar[c] & 0xFFFFFFFFu));
+                ++added;
+            }
+        }
+        if (!added) break;
+    }
+    const uint32_t cells = static_cast<uint32_t>(lrows.size());
+    T.cells = cells;
+    if (cells > 2) {
+        DevBuf pd;
+        KNN_TRY(pd.alloc(static_cast<size_t>(cells) * cells * 4));
+        tc_pair_d2_kernel<<<static_cast<uint32_t>((static_cast<uint64_t>(cells) * cells + 255) / 256), 256, 0, s>>>(
+            T.land.as<float>(), ps, dims, cells, pd.as<float>());
+        KNN_LAUNCHED();
+        std::vector<float> hd(static_cast<size_t>(cells) * cells);
+        KNN_TRY_CUDA(cudaMemcpyAsync(hd.data(), pd.ptr, hd.size() * 4, cudaMemcpyDeviceToHost, s));
+        KNN_TRY_CUDA(cudaStreamSynchronize(s));
+        std::vector<uint8_t> seen(cells, 0);
+        std::vector<uint32_t> chain{0};
+        seen[0] = 1;
+        for (uint32_t step = 1; step < cells; ++step) {
+            const float* row = hd.data() + static_cast<size_t>(chain.back()) * cells;
+            uint32_t best = kNone;
+            for (uint32_t j = 0; j < cells; ++j)
+                if (!seen[j] && (best == kNone || row[j] < row[best])) best = j;
+            seen[best] = 1;
+            chain.push_back(best);
+        }
+        std::vector<uint32_t> reordered(cells);
+        for (uint32_t i = 0; i < cells; ++i) reordered[i] = lrows[chain[i]];
+        lrows.swap(reordered);
+        KNN_TRY(place_landmarks());
+    }
+
+    // Farthest squared distance from each final landmark to its cell's points (query seeds).
+    KNN_TRY_CUDA(cudaMemsetAsync(far, 0, cells * 8ull, s));
+    tc_cell_far_kernel<<<ceil_div(n, 256), 256, 0, s>>>(src, stride, dims, k0, n, T.land.as<float>(), ps, far);
+    KNN_LAUNCHED();
+    {
+        std::vector<unsigned long long> hfar(cells);
+        KNN_TRY_CUDA(cudaMemcpyAsync(hfar.data(), far, cells * 8ull, cudaMemcpyDeviceToHost, s));
+        KNN_TRY_CUDA(cudaStreamSynchronize(s));
+        std::vector<float> cf(cells);
+        for (uint32_t c = 0; c < cells; ++c) {
+            const uint32_t bits = static_cast<uint32_t>(hfar[c] >> 32);
+            std::memcpy(&cf[c], &bits, 4);
+        }
+        KNN_TRY(T.cell_far.alloc(cells * 4ull));
+        KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_far.ptr, cf.data(), cells * 4ull, cudaMemcpyHostToDevice, s));
+        KNN_TRY_CUDA(cudaStreamSynchronize(s));
+    }
+
+    // Points by cell (stable), each cell's rows filling whole tiles.
+    bool alt = false;
+    KNN_TRY(radix_sort_pairs(k0, v0, k1, v1, n, static_cast<int>(log2_ceil(cells + 1)), st, s, &alt));
+    const uint32_t* keys = alt ? k1 : k0;
+    const uint32_t* vals = alt ? v1 : v0;
+    std::vector<uint32_t> hkeys(n);
+    KNN_TRY_CUDA(cudaMemcpyAsync(hkeys.data(), keys, n * 4ull, cudaMemcpyDeviceToHost, s));
+    KNN_TRY_CUDA(cudaStreamSynchronize(s));
+    std::vector<uint32_t> cell_start(cells + 1, 0), cell_tile(cells + 1, 0);
+    for (uint32_t i = 0; i < n; ++i) cell_start[hkeys[i] + 1]++;
+    for (uint32_t c = 0; c < cells; ++c) {
+        cell_tile[c + 1] = cell_tile[c] + ceil_div(cell_start[c + 1], kTileN);
+        cell_start[c + 1] += cell_start[c];
+    }
+    const uint32_t ptiles = cell_tile[cells];
+    const uint32_t prows = ptiles * kTileN;
+    const uint32_t ctiles = ceil_div(cells, kTileN);
+    T.ptiles = ptiles;
+    T.ctiles = ctiles;
+    DevBuf rowmap;
+    KNN_TRY(T.cell_start.alloc((cells + 1) * 4ull));
+    KNN_TRY(T.cell_tile.alloc((cells + 1) * 4ull));
+    KNN_TRY(rowmap.alloc(prows * 4ull));
+    KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_start.ptr, cell_start.data(), (cells + 1) * 4ull, cudaMemcpyHostToDevice, s));
+    KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_tile.ptr, cell_tile.data(), (cells + 1) * 4ull, cudaMemcpyHostToDevice, s));
+    KNN_TRY_CUDA(cudaMemsetAsync(rowmap.ptr, 0xFF, prows * 4ull, s));
+    tc_place_kernel<<<ceil_div(n, 256), 256, 0, s>>>(keys, vals, n, T.cell_start.as<uint32_t>(),
+                                                     T.cell_tile.as<uint32_t>(), rowmap.as<uint32_t>());
+    KNN_LAUNCHED();
+
+    // Point operand image, norms, FP32 copy, ids, per-tile norm bounds.
+    KNN_TRY(T.img.alloc(static_cast<size_t>(ptiles) * b_bytes(H)));
+    KNN_TRY(T.norm.alloc(prows * 4ull));
+    KNN_TRY(T.pts.alloc(static_cast<size_t>(prows) * ps * 4));
+    KNN_TRY(T.ids.alloc(prows * 4ull));
+    KNN_TRY(T.pmax.alloc(ptiles * 4ull));
+    tc_pack_kernel<<<ceil_div(prows, 128), 128, 0, s>>>(src, stride, dims, rowmap.as<uint32_t>(), prows, nullptr, kTileN,
+                                                        H, T.f16, T.scale, T.img.as<uint8_t>(), T.norm.as<float>(),
+                                                        INFINITY, T.pts.as<float>(), ps, src_ids, T.ids.as<uint32_t>(),
+                                                        prows, small.as<int>() + 1);
+    KNN_LAUNCHED();
+    tc_tile_max_kernel<<<ceil_div(ptiles, 128), 128, 0, s>>>(T.norm.as<float>(), ptiles, rel_margin(dims),
+                                                             T.pmax.as<float>());
+    KNN_LAUNCHED();
+
+    // Cell centres and radii (scaled), their operand image and row data.
+    DevBuf cb;
+    KNN_TRY(cb.alloc(carve_bytes({static_cast<size_t>(cells) * ps * 4, cells * 4ull, ctiles * kTileN * 4ull})));
+    Carver cc(cb.ptr);
+    float* centre = cc.take<float>(static_cast<size_t>(cells) * ps);
+    float* radius = cc.take<float>(cells);
+    float* cnorm = cc.take<float>(static_cast<size_t>(ctiles) * kTileN);
+    tc_cell_ball_kernel<<<ceil_div(cells * 32, 128), 128, 0, s>>>(T.pts.as<float>(), ps, dims, T.scale, T.norm.as<float>(),
+                                                                  T.cell_tile.as<uint32_t>(), cells, rel_margin(dims),
+                                                                  centre, radius);
+    KNN_LAUNCHED();
+    KNN_TRY(T.cimg.alloc(static_cast<size_t>(ctiles) * b_bytes(H)));
+    KNN_TRY(T.cdata.alloc(static_cast<size_t>(ctiles) * kRowData * 4));
+    KNN_TRY(T.cmax.alloc(ctiles * 4ull));
+    tc_pack_kernel<<<ceil_div(ctiles * kTileN, 128), 128, 0, s>>>(centre, ps, dims, nullptr, cells, nullptr, kTileN, H,
+                                                                  T.f16, 1.0f, T.cimg.as<uint8_t>(), cnorm, INFINITY,
+                                                                  nullptr, 0, nullptr, nullptr, ctiles * kTileN,
+                                                                  small.as<int>() + 1);
+    KNN_LAUNCHED();
+    tc_cdata_kernel<<<ceil_div(ctiles * kTileN, 256), 256, 0, s>>>(cnorm, radius, cells, ctiles, T.cdata.as<float>());
+    KNN_LAUNCHED();
+    tc_tile_max_kernel<<<ceil_div(ctiles, 128), 128, 0, s>>>(cnorm, ctiles, rel_margin(dims), T.cmax.as<float>());
+    KNN_LAUNCHED();
+    int bad = 0;
+    KNN_TRY_CUDA(cudaMemcpyAsync(&bad, small.as<int>() + 1, 4, cudaMemcpyDeviceToHost, s));
+    KNN_TRY_CUDA(cudaStreamSynchronize(s));
+    if (bad) return fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: a point's norm is not finite");
+    T.usable = true;
+    ix->device_bytes += T.img.bytes + T.norm.bytes + T.pts.bytes + T.ids.bytes + T.pmax.bytes + T.cimg.bytes +
+                        T.cdata.bytes + T.cmax.bytes + T.land.bytes + T.cell_tile.bytes + T.cell_start.bytes;
     return KNN_OK;
 }
 
 template <int PS>
-static int rescore_k(knn_index* ix, const QueryArgs& a, const uint32_t* cand, const uint32_t* cnt, uint32_t cap,
-                     uint32_t* retry, uint32_t* retry_count, cudaStream_t s) {
-    switch (k_class(a.k)) {
-        case 8: return rescore<PS, 8>(ix, a, cand, cnt, cap, retry, retry_count, s);
-        case 16: return rescore<PS, 16>(ix, a, cand, cnt, cap, retry, retry_count, s);
-        case 32: return rescore<PS, 32>(ix, a, cand, cnt, cap, retry, retry_count, s);
-        case 64: return rescore<PS, 64>(ix, a, cand, cnt, cap, retry, retry_count, s);
-        default: return rescore<PS, 128>(ix, a, cand, cnt, cap, retry, retry_count, s);
-    }
+static int rescore(const RescoreArgs& ra, uint32_t count, cudaStream_t s) {
+    tc_rescore_kernel<PS><<<ceil_div(count, kRescoreWarps), 32 * kRescoreWarps, 0, s>>>(ra);
+    KNN_LAUNCHED();
+    return KNN_OK;
 }
 
+uint32_t tc_default_cap(uint32_t k) { return std::min(4096u, std::max(1024u, 16u * k)); }
+
 int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaStream_t s) {
-    const uint32_t H = ix->dims <= 64 ? 1 : 2;
+    const uint32_t H = halves(ix->dims);
     if (!tc_supported(ix->dims, a.k)) return fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: dims %u, k %u", ix->dims, a.k);
-    KNN_TRY(tc_prepare(ix, s));
+    QueryPlan plain = plan;
+    plain.timing = false;
+    plain.bf16 = false;
+    // An index the 16-bit formats cannot hold (non-finite norms) answers by its plain search.
+    const int prc = tc_prepare(ix, s);
+    if (prc == KNN_ERR_UNSUPPORTED) return query_structure(ix, a, plain, s);
+    KNN_TRY(prc);
+    const auto& T = ix->tc;
     const uint32_t nq = a.count;
     const uint32_t qtiles = ceil_div(nq, kTileM);
     const uint32_t qrows = qtiles * kTileM;
-    const uint32_t cap = plan.tc_cap ? plan.tc_cap : 4096;
-    const size_t qimg_bytes = static_cast<size_t>(qtiles) * H * kTileM * 128u;
-    KNN_TRY(ix->tc_ws.reserve(carve_bytes({qimg_bytes, static_cast<size_t>(qrows) * 8, static_cast<size_t>(nq) * cap * 4,
-                                           static_cast<size_t>(nq) * 4, static_cast<size_t>(nq) * 4, 256})));
-    Carver c(ix->tc_ws.ptr);
+    const uint32_t cap = plan.tc_cap ? plan.tc_cap : tc_default_cap(a.k);
+    const size_t qimg_bytes = static_cast<size_t>(qtiles) * a_bytes(H);
+    KNN_TRY(ix->tc.ws.reserve(carve_bytes({nq * 4ull, nq * 4ull, nq * 4ull, nq * 4ull, radix_sort_temp_bytes(nq),
+                                            qimg_bytes, qrows * 4ull, qtiles * 16ull,
+                                            static_cast<size_t>(nq) * cap * 4, static_cast<size_t>(nq) * cap * 4,
+                                            nq * 4ull, nq * 4ull, nq * 4ull, nq * 4ull, 256})));
+    Carver c(ix->tc.ws.ptr);
+    uint32_t* k0 = c.take<uint32_t>(nq);
+    uint32_t* v0 = c.take<uint32_t>(nq);
+    uint32_t* k1 = c.take<uint32_t>(nq);
+    uint32_t* v1 = c.take<uint32_t>(nq);
+    void* st = c.take<uint8_t>(radix_sort_temp_bytes(nq));
     uint8_t* qimg = c.take<uint8_t>(qimg_bytes);
-    float2* qnorm = c.take<float2>(qrows);
+    float* qnorm = c.take<float>(qrows);
+    uint32_t* qhome = c.take<uint32_t>(qtiles * 4ull);
     uint32_t* cand = c.take<uint32_t>(static_cast<size_t>(nq) * cap);
+    float* cand_v = c.take<float>(static_cast<size_t>(nq) * cap);
     uint32_t* cnt = c.take<uint32_t>(nq);
+    float* final_t = c.take<float>(nq);
     uint32_t* retry = c.take<uint32_t>(nq);
+    float* seed = c.take<float>(nq);
     uint32_t* small = c.take<uint32_t>(64);  // [0] retry count, [1] error flag
     KNN_TRY_CUDA(cudaMemsetAsync(small, 0, 64 * sizeof(uint32_t), s));
-    tc_pack_kernel<<<ceil_div(qrows, 128), 128, 0, s>>>(a.queries, nq, ix->dims, ix->dims, kTileM, H, qimg, qnorm, qrows,
-                                                        a.order, a.count_dev);
+
+    // Queries by cell (rows past the live count sort last), with a seed bound from their cell.
+    KNN_TRY(launch_assign(ix->dp, a.queries, ix->dims, ix->dims, nq, a.order, a.count_dev, T.land.as<float>(), T.ps,
+                          T.cells, k0, v0, s, T.cell_far.as<float>(), T.cell_start.as<uint32_t>(), a.k, seed));
+    bool alt = false;
+    KNN_TRY(radix_sort_pairs(k0, v0, k1, v1, nq, static_cast<int>(log2_ceil(T.cells + 1)), st, s, &alt));
+    const uint32_t* cell_sorted = alt ? k1 : k0;
+    const uint32_t* order = alt ? v1 : v0;
+    tc_pack_kernel<<<ceil_div(qrows, 128), 128, 0, s>>>(a.queries, ix->dims, ix->dims, order, nq, a.count_dev, kTileM, H,
+                                                        T.f16, T.scale, qimg, qnorm, 0.0f, nullptr, 0, nullptr, nullptr,
+                                                        qrows, nullptr);
+    KNN_LAUNCHED();
+    tc_home_kernel<<<ceil_div(qtiles, 128), 128, 0, s>>>(cell_sorted, a.count_dev, nq, T.cell_start.as<uint32_t>(),
+                                                         T.cell_tile.as<uint32_t>(), T.cells,
+                                                         std::max(2 * a.k, 512u), qtiles, qhome);
     KNN_LAUNCHED();
 
     TcParams p{};
     p.qimg = qimg;
-    p.pimg = ix->tc_img.as<uint8_t>();
+    p.pimg = T.img.as<uint8_t>();
+    p.cimg = T.cimg.as<uint8_t>();
     p.qnorm = qnorm;
-    p.pnorm = ix->tc_norm.as<float2>();
-    p.n = ix->n;
+    p.pnorm = T.norm.as<float>();
+    p.cdata = T.cdata.as<float>();
+    p.pmax = T.pmax.as<float>();
+    p.cmax = T.cmax.as<float>();
+    p.cell_tile = T.cell_tile.as<uint32_t>();
+    p.qhome = qhome;
+    p.cells = T.cells;
+    p.ctiles = T.ctiles;
     p.nq = nq;
-    p.ptiles = ceil_div(ix->n, kTileN);
-    const double u = 1.0 / 256.0, D = ix->dims;
-    p.c1 = static_cast<float>(2.0 * (2.0 * u + u * u + D * std::ldexp(1.0, -20)) * (1.0 + 1.0 / 128.0));
-    p.c2 = static_cast<float>((D + 8.0) * std::ldexp(1.0, -23));
-    p.g = rel_margin(ix->dims);
+    p.ksteps = ceil_div(ix->dims, 16);
+    p.idesc = T.f16 ? idesc_f16(kTileM, kTileN) : idesc_bf16(kTileM, kTileN);
+    p.b = make_bounds(ix->dims, T.f16, T.scale);
+    p.s2 = T.scale * T.scale;
     p.max_d2 = a.max_d2;
     p.radii = a.radii;
-    p.order = a.order;
+    p.seed = seed;
+    p.order = order;
     p.live_count = a.count_dev;
     p.k = a.k;
     p.cap = cap;
     p.cand = cand;
+    p.cand_v = cand_v;
     p.cand_count = cnt;
+    p.final_t = final_t;
+    p.counters = a.counters;
     p.error = reinterpret_cast<int*>(small + 1);
     const size_t smem = filter_launch_smem(H, a.k);
     auto kern = H == 1 ? tc_filter_kernel<1> : tc_filter_kernel<2>;
@@ -498,25 +1409,49 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     KNN_LAUNCHED();
     if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
 
-    switch (round_up4(ix->dp)) {
-        case 16: KNN_TRY(rescore_k<16>(ix, a, cand, cnt, cap, retry, small, s)); break;
-        case 32: KNN_TRY(rescore_k<32>(ix, a, cand, cnt, cap, retry, small, s)); break;
-        case 64: KNN_TRY(rescore_k<64>(ix, a, cand, cnt, cap, retry, small, s)); break;
-        case 128: KNN_TRY(rescore_k<128>(ix, a, cand, cnt, cap, retry, small, s)); break;
-        default: KNN_TRY(rescore_k<8>(ix, a, cand, cnt, cap, retry, small, s)); break;
+    RescoreArgs ra{};
+    ra.pts = T.pts.as<float>();
+    ra.ids = T.ids.as<uint32_t>();
+    ra.pnorm = T.norm.as<float>();
+    ra.pmax = T.pmax.as<float>();
+    ra.queries = a.queries;
+    ra.dims = ix->dims;
+    ra.nq = nq;
+    ra.cap = cap;
+    ra.k = a.k;
+    ra.max_d2 = a.max_d2;
+    ra.radii = a.radii;
+    ra.order = order;
+    ra.live_count = a.count_dev;
+    ra.cand = cand;
+    ra.cand_v = cand_v;
+    ra.cand_count = cnt;
+    ra.qnorm = qnorm;
+    ra.final_t = final_t;
+    ra.b = p.b;
+    ra.out_idx = a.out_idx;
+    ra.out_dist = a.out_dist;
+    ra.retry = retry;
+    ra.retry_count = small;
+    ra.counters = a.counters;
+    switch (T.ps) {
+        case 4: KNN_TRY(rescore<4>(ra, nq, s)); break;
+        case 8: KNN_TRY(rescore<8>(ra, nq, s)); break;
+        case 16: KNN_TRY(rescore<16>(ra, nq, s)); break;
+        case 32: KNN_TRY(rescore<32>(ra, nq, s)); break;
+        case 64: KNN_TRY(rescore<64>(ra, nq, s)); break;
+        default: KNN_TRY(rescore<128>(ra, nq, s)); break;
     }
-    // Queries whose candidates overflowed, or whose filter block gave up, take the plain path.
+    // Queries whose candidates overflowed, that the 16-bit format could not hold, or whose filter
+    // block gave up, take the plain search of the index.
     QueryArgs again = a;
     again.order = retry;
     again.count_dev = small;
-    QueryPlan plain = plan;
-    plain.timing = false;
-    plain.bf16 = false;
-    return bf_query(ix, again, plain, s);
+    return query_structure(ix, again, plain, s);
 }
 
 int tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* bad) {
-    const uint32_t H = dims <= 64 ? 1 : 2;
+    const uint32_t H = halves(dims);
     const uint32_t qn = kTileM, pn = kTileN;
     std::vector<float> hq(static_cast<size_t>(qn) * dims), hp(static_cast<size_t>(pn) * dims);
     uint32_t st = 12345;
@@ -527,57 +1462,57 @@ int tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* bad) {
     for (auto& v : hq) v = rnd();
     for (auto& v : hp) v = rnd();
     DevBuf buf;
-    const size_t ab = static_cast<size_t>(H) * kTileM * 128u, bb = static_cast<size_t>(H) * kTileN * 128u;
-    KNN_TRY(buf.alloc(carve_bytes({hq.size() * 4, hp.size() * 4, ab, bb, qn * 8ull, pn * 8ull, qn * pn * 4ull, 64})));
+    const size_t ab = a_bytes(H), bb = b_bytes(H);
+    KNN_TRY(buf.alloc(carve_bytes({hq.size() * 4, hp.size() * 4, ab, bb, qn * 4ull, pn * 4ull, qn * pn * 4ull, 64})));
     Carver c(buf.ptr);
     float* dq = c.take<float>(hq.size());
     float* dp = c.take<float>(hp.size());
     uint8_t* qimg = c.take<uint8_t>(ab);
     uint8_t* pimg = c.take<uint8_t>(bb);
-    float2* qnm = c.take<float2>(qn);
-    float2* pnm = c.take<float2>(pn);
+    float* qnm = c.take<float>(qn);
+    float* pnm = c.take<float>(pn);
     float* out = c.take<float>(static_cast<size_t>(qn) * pn);
     int* err = c.take<int>(16);
     KNN_TRY_CUDA(cudaMemcpy(dq, hq.data(), hq.size() * 4, cudaMemcpyHostToDevice));
     KNN_TRY_CUDA(cudaMemcpy(dp, hp.data(), hp.size() * 4, cudaMemcpyHostToDevice));
-    KNN_TRY_CUDA(cudaMemset(err, 0, 64));
-    tc_pack_kernel<<<1, 128, 0>>>(dq, qn, dims, dims, kTileM, H, qimg, qnm, qn);
-    tc_pack_kernel<<<2, 128, 0>>>(dp, pn, dims, dims, kTileN, H, pimg, pnm, pn);
-    const size_t smem = 1024 + ab + bb + 64;
-    auto kern = H == 1 ? tc_selftest_kernel<1> : tc_selftest_kernel<2>;
-    KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    kern<<<1, 128, smem>>>(qimg, pimg, out, err);
-    KNN_LAUNCHED_N(3);
-    KNN_TRY_CUDA(cudaDeviceSynchronize());
-    std::vector<float> ho(static_cast<size_t>(qn) * pn);
-    int herr = 0;
-    KNN_TRY_CUDA(cudaMemcpy(ho.data(), out, ho.size() * 4, cudaMemcpyDeviceToHost));
-    KNN_TRY_CUDA(cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost));
-    if (herr) return fail(KNN_ERR_DEVICE_LIMIT, "tensor-core self-test kernel timed out");
-    // Inputs are multiples of 1/250 with |x| <= 4, bf16-rounded; products and sums in double.
-    auto bf = [](float x) {
-        uint32_t u;
-        std::memcpy(&u, &x, 4);
-        const uint32_t lsb = (u >> 16) & 1u;
-        u = (u + 0x7FFFu + lsb) & 0xFFFF0000u;
-        float r;
-        std::memcpy(&r, &u, 4);
-        return r;
-    };
     double worst = 0;
     uint32_t nbad = 0;
-    for (uint32_t i = 0; i < qn; ++i)
-        for (uint32_t j = 0; j < pn; ++j) {
-            double ref = 0, mag = 0;
-            for (uint32_t d = 0; d < dims; ++d) {
-                const double t = static_cast<double>(bf(hq[i * dims + d])) * bf(hp[j * dims + d]);
-                ref += t;
-                mag += std::fabs(t);
+    std::vector<float> ho(static_cast<size_t>(qn) * pn);
+    for (int f16 = 0; f16 < 2; ++f16) {
+        KNN_TRY_CUDA(cudaMemset(err, 0, 64));
+        tc_pack_kernel<<<1, 128>>>(dq, dims, dims, nullptr, qn, nullptr, kTileM, H, f16 != 0, 1.0f, qimg, qnm, 0.0f,
+                                   nullptr, 0, nullptr, nullptr, qn, nullptr);
+        tc_pack_kernel<<<2, 128>>>(dp, dims, dims, nullptr, pn, nullptr, kTileN, H, f16 != 0, 1.0f, pimg, pnm, 0.0f,
+                                   nullptr, 0, nullptr, nullptr, pn, nullptr);
+        const size_t smem = 1024 + ab + bb + 64;
+        auto kern = H == 1 ? tc_selftest_kernel<1> : tc_selftest_kernel<2>;
+        KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        kern<<<1, 128, smem>>>(qimg, pimg, f16 ? idesc_f16(kTileM, kTileN) : idesc_bf16(kTileM, kTileN), out, err);
+        KNN_LAUNCHED_N(3);
+        KNN_TRY_CUDA(cudaDeviceSynchronize());
+        int herr = 0;
+        KNN_TRY_CUDA(cudaMemcpy(ho.data(), out, ho.size() * 4, cudaMemcpyDeviceToHost));
+        KNN_TRY_CUDA(cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost));
+        if (herr) return fail(KNN_ERR_DEVICE_LIMIT, "tensor-core self-test kernel timed out");
+        // Inputs are multiples of 1/250 with |x| <= 4; the reference rounds them to the operand
+        // format on the host and sums the products in double.
+        auto round16 = [&](float x) {
+            if (f16) return __half2float(__float2half_rn(x));
+            return __bfloat162float(__float2bfloat16_rn(x));
+        };
+        for (uint32_t i = 0; i < qn; ++i)
+            for (uint32_t j = 0; j < pn; ++j) {
+                double ref = 0, mag = 0;
+                for (uint32_t d = 0; d < dims; ++d) {
+                    const double t = static_cast<double>(round16(hq[i * dims + d])) * round16(hp[j * dims + d]);
+                    ref += t;
+                    mag += std::fabs(t);
+                }
+                const double e = std::fabs(ho[static_cast<size_t>(i) * pn + j] - ref) / std::max(mag, 1e-30);
+                worst = std::max(worst, e);
+                if (e > dims * std::ldexp(1.0, -20)) ++nbad;
             }
-            const double e = std::fabs(ho[static_cast<size_t>(i) * pn + j] - ref) / std::max(mag, 1e-30);
-            worst = std::max(worst, e);
-            if (e > dims * std::ldexp(1.0, -20)) ++nbad;
-        }
+    }
     *max_rel_err = static_cast<float>(worst);
     *bad = nbad;
     return KNN_OK;

@@ -111,7 +111,7 @@ int make_plan(const knn_index* ix, const knn_query_opts* o, knn::QueryPlan* p) {
     p->sh_stack = o->shmem_stack != 0;
     p->reorder = (o->flags & KNN_QF_KEEP_ORDER) == 0;
     p->timing = (o->flags & KNN_QF_TIMING) != 0;
-    p->bf16 = (o->flags & KNN_QF_BF16_FILTER) != 0 && ix->structure == KNN_BRUTE_FORCE;
+    p->bf16 = (o->flags & KNN_QF_BF16_FILTER) != 0;
     p->tc_cap = o->reserved;
     p->leaf_scan = o->leaf_scan;
     if (o->traversal > 1) return fail(KNN_ERR_INVALID_ARGUMENT, "traversal %u: 0 or 1", o->traversal);
@@ -120,14 +120,12 @@ int make_plan(const knn_index* ix, const knn_query_opts* o, knn::QueryPlan* p) {
     return KNN_OK;
 }
 
+// The tensor-core filter where the plan asks for it and its tile fits (k <= 100 at dims > 64),
+// else the structure's own search.
 int dispatch(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& plan, cudaStream_t s) {
     if (ix->n == 0) return knn::fill_empty_rows(a, s);
-    switch (ix->structure) {
-        case KNN_BRUTE_FORCE: return knn::bf_query(ix, a, plan, s);
-        case KNN_KD_TREE: return knn::kd_query(ix, a, plan, s);
-        case KNN_BALL_TREE: return knn::ball_query(ix, a, plan, s);
-        default: return fail(KNN_ERR_INVALID_ARGUMENT, "unknown structure");
-    }
+    if (plan.bf16 && knn::tc_supported(ix->dims, a.k)) return knn::bf_tc_query(ix, a, plan, s);
+    return knn::query_structure(ix, a, plan, s);
 }
 
 // Learned radius: seed each query's radius from the model and search.  Queries that found fewer
@@ -138,9 +136,9 @@ constexpr int kSeedRounds = 3;
 constexpr float kSeedGrowth = 16.0f;
 
 int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& plan, cudaStream_t s) {
-    // The tensor-core brute force tightens each query's bound from its own running upper bounds
-    // within the first tiles; a seed would only add retries, so it runs unseeded.
-    if (ix->structure == KNN_BRUTE_FORCE && plan.bf16) return dispatch(ix, a, plan, s);
+    // The tensor-core filter tightens each query's bound from its own cell's points before it
+    // skips tiles; a seed would only add retries, so it runs unseeded.
+    if (plan.bf16) return dispatch(ix, a, plan, s);
     const size_t n = a.count;
     const uint32_t* order = nullptr;
     if (plan.reorder && a.count >= 4096) {
@@ -188,7 +186,7 @@ int k_slot(uint32_t k) {
 // caller's queries (CUDA events, best of two runs each), in three stages: leaf bucket size,
 // then block size, then tracker/stack storage.  Results are exact for every candidate.
 int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t s, knn::QueryPlan* out,
-             float* best_ms, uint32_t* tried) {
+             float* best_ms, uint32_t* tried, bool allow_tc = true) {
     knn::QueryArgs t = a;
     // Brute force costs n distances per query; a smaller sample keeps tuning short.
     t.count = std::min<uint32_t>(a.count, ix->structure == KNN_BRUTE_FORCE ? 8192u : 32768u);
@@ -228,11 +226,14 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
         return KNN_OK;
     };
     do {
+        // The tensor-core filter, for dims >= 16 (the form it is built for), on any structure.
+        const bool try_tc = allow_tc && ix->dims >= 16 && knn::tc_supported(ix->dims, a.k);
         if (ix->structure != KNN_BRUTE_FORCE) {
             for (bool warp : {false, true}) {
                 for (uint32_t leaf : {0u, 4u, 8u, 16u, 32u, 64u}) {
                     if (leaf && leaf <= ix->leaf_slots) continue;
                     knn::QueryPlan p = best;
+                    p.bf16 = false;
                     p.warp = warp;
                     p.leaf_scan = leaf;
                     if ((rc = consider(p)) != KNN_OK) break;
@@ -240,10 +241,15 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
                 if (rc != KNN_OK) break;
             }
             if (rc != KNN_OK) break;
+            if (try_tc) {
+                knn::QueryPlan p;
+                p.block = 128;
+                p.bf16 = true;
+                if ((rc = consider(p)) != KNN_OK) break;
+            }
         } else {
             if ((rc = consider(best)) != KNN_OK) break;
-            // The BF16 tensor-core filter, for dims >= 16 (the brute-force form it is built for).
-            if (ix->dims >= 16 && knn::tc_supported(ix->dims, a.k)) {
+            if (try_tc) {
                 knn::QueryPlan p = best;
                 p.bf16 = true;
                 if ((rc = consider(p)) != KNN_OK) break;
@@ -280,11 +286,23 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
 }  // namespace
 
 namespace knn {
-// The autotuner's plan for one query batch on one index (used by batches).
+// The structure's own search (no tensor-core filter).
+int query_structure(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaStream_t s) {
+    if (ix->n == 0) return fill_empty_rows(a, s);
+    switch (ix->structure) {
+        case KNN_BRUTE_FORCE: return bf_query(ix, a, plan, s);
+        case KNN_KD_TREE: return kd_query(ix, a, plan, s);
+        case KNN_BALL_TREE: return ball_query(ix, a, plan, s);
+        default: return fail(KNN_ERR_INVALID_ARGUMENT, "unknown structure");
+    }
+}
+
+// The autotuner's plan for one query batch on one index, among the structure's own searches
+// (used by batches, whose persistent kernels run those).
 int tune_plan(knn_index* ix, const QueryArgs& a, cudaStream_t s, QueryPlan* out) {
     float ms = 0.0f;
     uint32_t tried = 0;
-    return autotune(ix, a, false, s, out, &ms, &tried);
+    return autotune(ix, a, false, s, out, &ms, &tried, false);
 }
 }  // namespace knn
 

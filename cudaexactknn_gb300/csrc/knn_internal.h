@@ -168,10 +168,27 @@ struct knn_index {
     knn::DevBuf points;
     uint32_t point_stride = 0;
 
-    // Brute force, tensor-core filter: BF16 point image (128-byte swizzle tiles of 256 points)
-    // and {|p|^2, |p|} per point, built on first use; scratch for the query images and candidates.
-    knn::DevBuf tc_img, tc_norm, tc_ws;
-    bool tc_ready = false;
+    // Tensor-core filter (bf_tc.cu), built on first use for any structure: the points grouped
+    // into landmark cells, laid out cell by cell in tiles of 256 rows (each cell's last tile
+    // padded), with
+    //   img    16-bit operand image (FP16 scaled by 2^e, or BF16), 128-byte swizzle, per tile
+    //   norm   squared norm of each scaled row (+inf on padding rows)
+    //   pts    FP32 coordinates per padded row (stride ps, zero padded) for exact rescoring
+    //   ids    index of each padded row in the caller's point array (0xFFFFFFFF on padding)
+    //   pmax   per tile: upper bound on the scaled norm of its rows
+    //   land   landmarks [cells][ps]; cell_start [cells + 1] first sorted point of each cell;
+    //          cell_tile [cells + 1] first tile of each cell; cell_far [cells] float squared
+    //          distance from each landmark to its farthest point
+    //   cimg, cdata, cmax  the cell centres as a 16-bit operand image, per centre tile their
+    //          norms and radii (scaled), and an upper bound on the centres' norms
+    struct TensorCoreState {
+        knn::DevBuf img, norm, pts, ids, pmax, land, cell_start, cell_tile, cell_far, cimg, cdata, cmax, ws;
+        uint32_t cells = 0, ptiles = 0, ctiles = 0, ps = 0;
+        bool f16 = true;
+        float scale = 1.0f;   // power of two applied before rounding to FP16
+        bool ready = false;   // built
+        bool usable = false;  // built and every scaled norm finite
+    } tc;
 
     // k-d tree: split value per internal node (implicit heap, children 2i+1, 2i+2).
     knn::DevBuf split;
@@ -259,7 +276,9 @@ int model_train(knn_index* ix, const float* d_samples, uint32_t count, uint32_t 
                 cudaStream_t s, knn_train_report* rep);
 
 int bf_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
-// Brute force through the BF16 tensor-core filter (bf_tc.cu).
+// The structure's own search, without the tensor-core filter (capi.cu).
+int query_structure(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
+// Any index through the 16-bit tensor-core filter with tile skipping (bf_tc.cu).
 bool tc_supported(uint32_t dims, uint32_t k);
 int tc_prepare(knn_index* ix, cudaStream_t s);
 int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);

@@ -1,7 +1,8 @@
-"""Brute force through the BF16 tensor-core filter (tcgen05) with exact FP32 rescoring.
+"""Queries through the 16-bit tensor-core filter (tcgen05: FP16 with power-of-two scaling, or
+BF16 for wide data), cell-ordered tiles with ball-bound tile skipping, and exact FP32 rescoring.
 
 The filter is only a filter: every returned row must equal the plain brute force's exactly
-(same keys: indices, tie order and distance bits), whatever the data, k or radius."""
+(same keys: indices, tie order and distance bits), whatever the index, data, k or radius."""
 
 import ctypes
 
@@ -22,7 +23,7 @@ def _flags():
 
 @pytest.mark.parametrize("dims", [16, 40, 64, 100, 128])
 def test_tensor_core_selftest(dims):
-    """tcgen05.mma over one 128x256 tile matches exact products of the BF16 inputs."""
+    """tcgen05.mma over one 128x256 tile matches exact products of the FP16 and BF16 inputs."""
     from cudaexactknn_gb300 import _lib
     err = ctypes.c_float()
     bad = ctypes.c_uint32()
@@ -85,3 +86,59 @@ def test_filter_with_learned_radius():
     want = oracle.bf_knn(pts, qs, 50, fma=True, threads=8)
     got = gu.run(ix, qs, 50, flags=_flags() | _lib.QF_LEARNED_RADIUS)
     gu.assert_rows_equal(*got, *want, what="bf16 filter + learned radius")
+
+
+@pytest.mark.parametrize("structure,dims,k", [("kd", 16, 8), ("kd", 20, 32), ("ball", 16, 32), ("ball", 32, 10),
+                                              ("ball", 100, 64)])
+def test_filter_on_trees(structure, dims, k):
+    """Trees answer through the same filter (their leaf slots are the point set)."""
+    rng = np.random.default_rng(dims * 7 + k)
+    pts, basis = W.subspace(rng, 30000, dims, 4, 0.05)
+    qs, _ = W.subspace(rng, 2000, dims, 4, 0.05, basis)
+    ix = gu.make_index(structure, pts)
+    for r2 in (float("inf"), 0.5):
+        want = oracle.bf_knn(pts, qs, k, r2, fma=True, threads=8)
+        gu.assert_rows_equal(*gu.run(ix, qs, k, r2, flags=_flags()), *want, what=f"{structure} D={dims} k={k} r2={r2}")
+
+
+def test_clustered_data_skips_tiles():
+    """Well separated clusters: most point tiles are skipped, answers stay exact."""
+    from cudaexactknn_gb300 import knn
+    rng = np.random.default_rng(11)
+    pts, centres = W.gauss_mix(rng, 60000, 64, 64, 0.1)
+    qs, _ = W.gauss_mix(rng, 2048, 64, 64, 0.1, centres)
+    ix = gu.make_index("bf", pts)
+    want = oracle.bf_knn(pts, qs, 20, fma=True, threads=8)
+    gu.assert_rows_equal(*gu.run(ix, qs, 20, flags=_flags()), *want, what="clustered")
+    c = ix.stats(knn.Query(gu.to_dev(qs), len(qs), float("inf")), 20, flags=_flags())
+    full_scan = (len(qs) // 128) * (60000 // 256)  # point tiles a brute-force pass would scan
+    assert 0 < c.leaves_visited < full_scan // 4, (c.leaves_visited, full_scan)
+    assert c.fallback_queries == 0
+    assert c.nodes_visited >= len(qs) * 20  # candidates rescored
+
+
+@pytest.mark.parametrize("scale", [1e-20, 1e-3, 1e5, 1e30])
+def test_filter_magnitudes(scale):
+    """Tiny data (large FP16 scale), huge data (BF16 format): exact either way."""
+    rng = np.random.default_rng(12)
+    pts, centres = W.gauss_mix(rng, 5000, 24, 16, 0.3)
+    qs, _ = W.gauss_mix(rng, 400, 24, 16, 0.3, centres)
+    pts = (pts * np.float32(scale)).astype(np.float32)
+    qs = (qs * np.float32(scale)).astype(np.float32)
+    ix = gu.make_index("bf", pts)
+    want = oracle.bf_knn(pts, qs, 12, fma=True, threads=8)
+    gu.assert_rows_equal(*gu.run(ix, qs, 12, flags=_flags()), *want, what=f"scale {scale}")
+
+
+def test_queries_outside_the_format_fall_back():
+    """Queries whose scaled coordinates overflow FP16 take the plain search, exactly."""
+    from cudaexactknn_gb300 import knn
+    rng = np.random.default_rng(13)
+    pts = W.uniform(rng, 4000, 32)
+    qs = W.uniform(rng, 300, 32)
+    qs[::7] *= np.float32(1e6)
+    ix = gu.make_index("bf", pts)
+    want = oracle.bf_knn(pts, qs, 10, fma=True, threads=8)
+    gu.assert_rows_equal(*gu.run(ix, qs, 10, flags=_flags()), *want, what="fp16 overflow queries")
+    c = ix.stats(knn.Query(gu.to_dev(qs), len(qs), float("inf")), 10, flags=_flags())
+    assert c.fallback_queries == len(range(0, 300, 7))
