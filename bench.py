@@ -199,6 +199,22 @@ def algorithmic_bytes(w, counters, count):
     return total, floor
 
 
+def fp64_error(w, rows, idx, dist):
+    """Largest error of the returned FP32 squared distances against the same pairs summed in
+    FP64 on the host: absolute, relative, and the bound (D + 4) 2^-23 relative."""
+    valid = idx >= 0
+    if not valid.any():
+        return None
+    q = np.repeat(w.queries[rows].astype(np.float64), idx.shape[1], axis=0)[valid.ravel()]
+    p = w.points[idx[valid]].astype(np.float64)
+    exact = ((q - p) ** 2).sum(axis=1)
+    got = dist[valid].astype(np.float64)
+    err = np.abs(got - exact)
+    rel = err[exact > 0] / exact[exact > 0]
+    return {"max_abs": float(err.max()), "max_rel": float(rel.max()) if rel.size else 0.0,
+            "bound_rel": (w.dims + 4) * 2.0 ** -23, "pairs": int(valid.sum())}
+
+
 def cpu_baseline(w, threads, sample=None):
     import oracle
     qs = w.queries if sample is None else w.queries[:sample]
@@ -521,6 +537,7 @@ def main():
         index.batch_knn(query, k, **kw)
         got = oracle.row_keys(out_i[sample].cpu().numpy(), out_d[sample].cpu().numpy())
         exact[name] = float((got == want).all(axis=1).mean())
+    fp64 = fp64_error(w, sample, out_i[sample].cpu().numpy(), out_d[sample].cpu().numpy())
 
     counters = index.stats(query, k, **plain_kw)
     alg_bytes, floor_bytes = algorithmic_bytes(w, counters, count)
@@ -564,10 +581,12 @@ def main():
 
     kernel_name = {"kd": "kd_knn_kernel", "ball": "ball_knn_kernel", "bf": "bf_knn_kernel"}[w.structure]
     if tuned_plan.get("bf16_filter"):
-        # Brute force through the tensor cores: 2 N D flops per query in the BF16 GEMM.
+        # Tensor-core filter: the MMA work it issues, 2 x 128 queries x 256 rows x (16 per K step,
+        # ceil(D/16) steps) per point tile scanned (device counter), against the dense 16-bit peak.
         kernel_name = "tc_filter_kernel"
         peak, peak_kind = bf16_peak()
-        flops = 2.0 * w.points.shape[0] * w.dims * count
+        mma_tiles = int(chosen_counters.leaves_visited)
+        flops = 2.0 * 128 * 256 * 16 * math.ceil(w.dims / 16) * mma_tiles
         achieved = flops / (chosen_kern_ms / 1e3) / 1e12
         roof_bound, roof_unit = "tensor", "TFLOP/s"
     else:
@@ -585,6 +604,7 @@ def main():
                    "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
         "exact_match": {"chosen": exact["chosen"], "plain": exact["plain"], "e2e": e2e_exact,
                         "sample_queries": int(len(sample))},
+        "distance_error_vs_fp64": fp64,
         "plain": {"value": plain_qps, "ms_per_step": plain_ms / args.steps, "plan": plain_kw,
                   "kernel_ms": plain_kern_ms},
         "chosen": {"form": "autotune + learned radius" if learned else "autotune", "plan": tuned_plan,
@@ -602,6 +622,7 @@ def main():
                 "d2h_bytes_per_step": int(count * k * 8)},
         "gpu_launches": int(launches),
         "roofline": {"bound": roof_bound, "achieved": achieved, "peak": peak, "unit": roof_unit,
+                     "mma_tiles_scanned": int(chosen_counters.leaves_visited) if tuned_plan.get("bf16_filter") else None,
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"{peak_kind} " + ("bf16_tflops" if roof_bound == "tensor" else "hbm_gbs"),
                      "kernel": kernel_name, "algorithmic_bytes_per_launch": int(alg_bytes),

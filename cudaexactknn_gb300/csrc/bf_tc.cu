@@ -77,12 +77,15 @@ constexpr uint32_t kTileM = 128;
 constexpr uint32_t kTileN = 256;
 constexpr uint32_t kEpiWarps = 4;
 constexpr uint32_t kThreads = 32 * (2 + kEpiWarps);
-constexpr uint32_t kTmemCols = 512;  // two accumulators of kTileN fp32 columns
 constexpr uint32_t kCellPoints = 1024;
 constexpr uint32_t kMaxCells = 4096;
 constexpr uint32_t kMaskWords = kMaxCells / 32;
 constexpr uint32_t kRowData = 2 * kTileN;  // floats of row data per tile: norms, then (centres) radii
 constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr uint32_t kStage = 16;               // accumulator values staged per thread for its hits
+constexpr uint32_t kCentreBit = 0x80000000u;  // item code: a centre tile
+constexpr uint32_t kBoundary = 0xFFFFFFFEu;   // item code: centre tiles done, mask next
+constexpr uint32_t kEnd = 0xFFFFFFFDu;        // item code: no more items
 
 __host__ __device__ __forceinline__ uint32_t a_bytes(uint32_t h) { return h * kTileM * 128u; }
 __host__ __device__ __forceinline__ uint32_t b_bytes(uint32_t h) { return h * kTileN * 128u; }
@@ -203,8 +206,12 @@ struct TileSeq {
 
 __device__ __forceinline__ void epilogue_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(kEpiWarps * 32) : "memory"); }
 
-template <uint32_t H>
+// ACC accumulators of kTileN TMEM columns: 2 lets the MMAs of the next tile run while the
+// epilogue drains this one (one block per SM); 1 leaves room for two blocks per SM, whose
+// epilogues then hide each other's latencies.
+template <uint32_t H, uint32_t ACC>
 __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p) {
+    constexpr uint32_t kCols = ACC * kTileN;
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte alignment for the 128-byte swizzle atoms.
     const uint32_t raw = smem_addr(smem_raw);
@@ -214,7 +221,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     uint8_t* sB1 = sB0 + b_bytes(H);
     float* sN = reinterpret_cast<float*>(sB1 + b_bytes(H));       // [2][kRowData] row data
     uint32_t* sMask = reinterpret_cast<uint32_t*>(sN + 2 * kRowData);  // [kMaskWords] kept cells
-    float* heap_base = reinterpret_cast<float*>(sMask + kMaskWords);   // [k][kTileM]
+    uint32_t* sItem = sMask + kMaskWords;                              // [2] item code per stage
+    float* sMeta = reinterpret_cast<float*>(sItem + 2);                // [2] its norm bound (Pmax/Cmax)
+    float* sStage = sMeta + 2;                                         // [kStage][kTileM] staged sums
+    float* heap_base = sStage + kStage * kTileM;                       // [k][kTileM]
     uint64_t* bars = reinterpret_cast<uint64_t*>(heap_base + static_cast<size_t>(p.k) * kTileM);
     uint64_t* full = bars;            // [2] tile (operands + row data) landed
     uint64_t* empty = bars + 2;       // [2] operands consumed by the MMAs
@@ -251,26 +261,32 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         *abort = 0;
         mbar_fence_init();
     }
-    if (warp == 1) tmem_alloc(tmem_slot, kTmemCols);
+    if (warp == 1) tmem_alloc(tmem_slot, kCols);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
+    // The producer walks the tile sequence and publishes each stage's item in shared memory
+    // (sItem: tile index, kCentreBit for centre tiles, or a marker) before its arrival on `full`;
+    // the MMA issuer and the epilogue take the items from there, in order.
     if (warp == 0) {
         if (lane == 0) {
-            // Producer: the query tile once, then the tile sequence through the 2-stage ring.
             mbar_expect_tx(a_full, a_bytes(H));
             bulk_copy_g2s(sA, p.qimg + static_cast<size_t>(qt) * a_bytes(H), a_bytes(H), a_full);
             uint32_t issued = 0, data_tiles = 0;
+            auto stage_free = [&](uint32_t s) -> bool {
+                // Stage s is free once the MMAs of item issued-2 are done (operands) and the
+                // epilogue has drained it (row data).
+                if (issued < 2) return true;
+                const uint32_t par = ((issued >> 1) - 1) & 1;
+                return mbar_wait(empty + s, par, abort) && mbar_wait(acc_empty + s, par, abort);
+            };
             auto load = [&](uint32_t item, bool centre) -> bool {
                 const uint32_t s = issued & 1;
-                // Stage s is free once the MMAs of load issued-2 are done (operands) and the
-                // epilogue has drained it (row data).
-                if (issued >= 2) {
-                    const uint32_t par = ((issued >> 1) - 1) & 1;
-                    if (!mbar_wait(empty + s, par, abort) || !mbar_wait(acc_empty + s, par, abort)) return false;
-                }
+                if (!stage_free(s)) return false;
+                sItem[s] = item | (centre ? kCentreBit : 0u);
+                sMeta[s] = centre ? __ldg(p.cmax + item) : __ldg(p.pmax + item);
                 const uint32_t rd_bytes = (centre ? kRowData : kTileN) * sizeof(float);
                 mbar_expect_tx(full + s, b_bytes(H) + rd_bytes);
                 const uint8_t* img = centre ? p.cimg : p.pimg;
@@ -282,14 +298,23 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 data_tiles += centre ? 0u : 1u;
                 return true;
             };
+            auto marker = [&](uint32_t code) -> bool {
+                const uint32_t s = issued & 1;
+                if (!stage_free(s)) return false;
+                sItem[s] = code;
+                mbar_arrive(full + s);
+                ++issued;
+                return true;
+            };
             bool ok = true;
             uint32_t item;
             bool centre;
             for (uint32_t st = 0; ok && st < 3; ++st) {
-                if (st == 2) ok = mbar_wait(mask_ready, 0, abort) && !*abort;
+                if (st == 2) ok = marker(kBoundary) && mbar_wait(mask_ready, 0, abort) && !*abort;
                 seq.begin(st);
                 while (ok && seq.next(&item, &centre)) ok = load(item, centre);
             }
+            ok = ok && marker(kEnd);
             if (!ok) {
                 *abort = 1;
                 // Let copies in flight land before the block can exit.
@@ -302,38 +327,44 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            // MMA issuer.
+            // MMA issuer: one accumulator per item; markers pass through.
             const uint32_t a0 = smem_addr(sA);
-            uint32_t i = 0;
-            auto mma_tile = [&]() -> bool {
-                const uint32_t s = i & 1;
-                if (!mbar_wait(full + s, (i >> 1) & 1, abort)) return false;
-                if (i >= 2 && !mbar_wait(acc_empty + s, ((i >> 1) - 1) & 1, abort)) return false;
-                tc_fence_after();
-                const uint32_t b0 = smem_addr(s ? sB1 : sB0);
-                for (uint32_t ks = 0; ks < p.ksteps; ++ks) {
-                    const uint32_t h = ks >> 2, kk = ks & 3;
-                    mma_f16kind(tmem + s * kTileN, desc_sw128(a0 + h * kTileM * 128u + kk * 32u),
-                                desc_sw128(b0 + h * kTileN * 128u + kk * 32u), p.idesc, ks != 0);
-                }
-                mma_commit(empty + s);
-                mma_commit(acc_full + s);
-                ++i;
-                return true;
-            };
+            uint32_t i = 0, last_mma = kNone;
             bool ok = mbar_wait(a_full, 0, abort);
-            uint32_t item;
-            bool centre;
-            for (uint32_t st = 0; ok && st < 3; ++st) {
-                if (st == 2) ok = mbar_wait(mask_ready, 0, abort) && !*abort;
-                seq.begin(st);
-                while (ok && seq.next(&item, &centre)) ok = mma_tile();
+            while (ok) {
+                const uint32_t s = i & 1;
+                // The accumulator this item writes is free once the epilogue has drained the item
+                // that used it last: item i-2 (two accumulators) or i-1 (one).
+                const uint32_t prev = i - ACC;
+                if (!mbar_wait(full + s, (i >> 1) & 1, abort) ||
+                    (i >= ACC && !mbar_wait(acc_empty + (prev & 1), (prev >> 1) & 1, abort))) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t code = sItem[s];
+                if (code == kBoundary || code == kEnd) {
+                    mbar_arrive(empty + s);
+                    mbar_arrive(acc_full + s);
+                } else {
+                    tc_fence_after();
+                    const uint32_t b0 = smem_addr(s ? sB1 : sB0);
+                    for (uint32_t ks = 0; ks < p.ksteps; ++ks) {
+                        const uint32_t h = ks >> 2, kk = ks & 3;
+                        mma_f16kind(tmem + (ACC == 2 ? s * kTileN : 0u), desc_sw128(a0 + h * kTileM * 128u + kk * 32u),
+                                    desc_sw128(b0 + h * kTileN * 128u + kk * 32u), p.idesc, ks != 0);
+                    }
+                    mma_commit(empty + s);
+                    mma_commit(acc_full + s);
+                    last_mma = i;
+                }
+                ++i;
+                if (code == kEnd) break;
             }
             if (!ok) {
                 *abort = 1;
                 // The MMAs already issued finish before TMEM is released.
                 volatile int never = 0;
-                if (i) mbar_wait(acc_full + ((i - 1) & 1), ((i - 1) >> 1) & 1, &never);
+                if (last_mma != kNone) mbar_wait(acc_full + (last_mma & 1), (last_mma >> 1) & 1, &never);
             }
         }
     } else {
@@ -369,14 +400,26 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         float* my_v = p.cand_v + static_cast<size_t>(live ? r : 0) * p.cap;
         const uint32_t taddr_row = tmem + ((quarter * 32u) << 16);
         uint32_t i = 0;
-        auto process = [&](uint32_t item, bool centre) -> bool {
+        // Takes the next item (waits for its accumulator and row data); false on failure.
+        auto take = [&](uint32_t* code) -> bool {
             const uint32_t s = i & 1;
-            // The TMEM loads below are warp-collective: the whole warp proceeds or leaves.
+            // The TMEM loads that follow are warp-collective: the whole warp proceeds or leaves.
             const bool got = mbar_wait(acc_full + s, (i >> 1) & 1, abort) && mbar_wait(full + s, (i >> 1) & 1, abort);
             if (!__all_sync(0xFFFFFFFFu, got)) return false;
             tc_fence_after();
+            *code = sItem[s];
+            return true;
+        };
+        auto release = [&]() {
+            tc_fence_before();
+            mbar_arrive(acc_empty + (i & 1));
+            ++i;
+        };
+        auto process = [&](uint32_t item, bool centre) {
+            const uint32_t s = i & 1;
+            const float meta = sMeta[s];
             const float* rd = sN + s * kRowData;
-            const uint32_t tcol = taddr_row + s * kTileN;
+            const uint32_t tcol = taddr_row + (ACC == 2 ? s * kTileN : 0u);
             // Chunks of 32 accumulator columns; the TMEM load of chunk c+1 is in flight while
             // chunk c is processed.
             uint32_t ra[32], rb[32];
@@ -384,7 +427,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
             tmem_wait_ld(ra);
             if (centre) {
                 // Cell test: keep cell c when S_lo(q, c) <= (R_c + t)^2 for some query.
-                const float Ec = bound_e(__ldg(p.cmax + item));
+                const float Ec = bound_e(meta);
                 const float base = __fsub_rd(__fmul_rd(one_m_gn, nq), __fmul_ru(2.0f, Ec));
                 const float t2 = __fmul_ru(__fadd_ru(T, b.c4), b.inv_one_m);
                 const float tq = __fsqrt_ru(t2);
@@ -416,54 +459,57 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                     if (c + 2 < kTileN / 32) tmem_wait_ld(ra);
                 }
             } else {
-                E = bound_e(__ldg(p.pmax + item));
+                E = bound_e(meta);
                 theta0 = __fsub_rd(a_q, E);
                 set_theta();
                 const float E2 = __fmul_ru(2.0f, E);
                 const float4* pn4 = reinterpret_cast<const float4*>(rd);
                 const uint32_t base = item * kTileN;
+                float* stage = sStage + row;  // slot x at stage[x * kTileM]
                 auto chunk = [&](const uint32_t (&r)[32], uint32_t c) {
-                    // The hit mask first, branch-free; then this lane's hits: recorded, and folded
-                    // into the bound heap afterwards so that lanes with hits update side by side
-                    // (theta is up to one chunk stale, which only keeps extra candidates).
-                    uint32_t m = 0;
+                    // Per half chunk of 16 columns: the hit mask first, branch-free; then each
+                    // lane walks its own hits (lanes side by side), recording candidates and folding
+                    // their distance upper bounds into its heap (theta is refreshed once per half
+                    // chunk, which only keeps extra candidates).
 #pragma unroll
-                    for (uint32_t j4 = 0; j4 < 8; ++j4) {
-                        const float4 n4 = pn4[c * 8 + j4];
-                        const float nn[4] = {n4.x, n4.y, n4.z, n4.w};
+                    for (uint32_t half = 0; half < 2; ++half) {
+                        uint32_t m = 0;
 #pragma unroll
-                        for (uint32_t e = 0; e < 4; ++e)
-                            m |= (__fmaf_ru(-a, nn[e], __uint_as_float(r[j4 * 4 + e])) >= theta) ? (1u << (j4 * 4 + e)) : 0u;
-                    }
-                    if (m == 0) return;
-                    float hv[32], hn[32];
-                    uint32_t nh = 0;
+                        for (uint32_t j4 = 0; j4 < 4; ++j4) {
+                            const float4 n4 = pn4[c * 8 + half * 4 + j4];
+                            const float nn[4] = {n4.x, n4.y, n4.z, n4.w};
 #pragma unroll
-                    for (uint32_t j = 0; j < 32; ++j) {
-                        if (m & (1u << j)) {
-                            const float vj = __uint_as_float(r[j]);
+                            for (uint32_t e = 0; e < 4; ++e) {
+                                const uint32_t j = half * 16 + j4 * 4 + e;
+                                m |= (__fmaf_ru(-a, nn[e], __uint_as_float(r[j])) >= theta) ? (1u << j) : 0u;
+                            }
+                        }
+                        if (m == 0) continue;
+                        // This lane's 16 sums go to shared memory so that its hits can be taken
+                        // bit by bit (registers cannot be indexed at run time).
+#pragma unroll
+                        for (uint32_t jj = 0; jj < 16; ++jj) stage[jj * kTileM] = __uint_as_float(r[half * 16 + jj]);
+                        bool moved = false;
+                        while (m) {
+                            const uint32_t j = static_cast<uint32_t>(__ffs(m) - 1);
+                            m &= m - 1u;
+                            const float vj = stage[(j - half * 16) * kTileM];
                             if (count < p.cap) {
                                 my_cand[count] = base + c * 32 + j;
                                 my_v[count] = vj;
                             }
                             ++count;
-                            hv[nh] = vj;
-                            hn[nh] = rd[c * 32 + j];
-                            ++nh;
+                            // Upper bound of this pair's float distance (scaled).
+                            const float hi = __fmaf_ru(-2.0f, vj, __fadd_ru(E2, __fmul_ru(up_n, __fadd_ru(nq, rd[c * 32 + j]))));
+                            const float u = __fmul_ru(fmaxf(hi, 0.0f), up_g);
+                            if (u < T) {
+                                heap.replace_top(u);
+                                T = heap.at(0);
+                                moved = true;
+                            }
                         }
+                        if (moved) set_theta();
                     }
-                    bool moved = false;
-                    for (uint32_t x = 0; x < nh; ++x) {
-                        // Upper bound of this pair's float distance (scaled).
-                        const float hi = __fmaf_ru(-2.0f, hv[x], __fadd_ru(E2, __fmul_ru(up_n, __fadd_ru(nq, hn[x]))));
-                        const float u = __fmul_ru(fmaxf(hi, 0.0f), up_g);
-                        if (u < T) {
-                            heap.replace_top(u);
-                            T = heap.at(0);
-                            moved = true;
-                        }
-                    }
-                    if (moved) set_theta();
                 };
                 // (The TMEM loads and waits are warp-collective: the warp reconverges before each.)
 #pragma unroll 1
@@ -478,32 +524,36 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                     if (c + 2 < kTileN / 32) tmem_wait_ld(ra);
                 }
             }
-            tc_fence_before();
-            mbar_arrive(acc_empty + s);
-            ++i;
-            return true;
         };
-        bool ok = true;
-        uint32_t item;
-        bool centre;
-        for (uint32_t st = 0; ok && st < 2; ++st) {
-            seq.begin(st);
-            while (ok && seq.next(&item, &centre)) ok = process(item, centre);
+        // Items until the end marker; at the boundary marker (every centre tile done) the
+        // epilogue warps complete the kept-cell mask and release the producer into phase 2.  A
+        // warp that fails still joins that barrier (once) before it leaves.
+        bool ok = true, boundary_done = false;
+        auto boundary = [&]() {
+            epilogue_barrier();
+            mbar_arrive(mask_ready);
+            boundary_done = true;
+        };
+        for (;;) {
+            uint32_t code = 0;
+            if (!take(&code)) {
+                ok = false;
+                break;
+            }
+            if (code == kEnd) break;
+            if (code == kBoundary) {
+                release();
+                boundary();
+                continue;
+            }
+            process(code & ~kCentreBit, (code & kCentreBit) != 0);
+            release();
         }
         if (!ok) *abort = 1;
-        // Every epilogue thread reaches the barrier (the mask is complete after it) and arrives on
-        // mask_ready, failed or not; a failure seen here stops all roles.
-        epilogue_barrier();
-        mbar_arrive(mask_ready);
-        ok = __all_sync(0xFFFFFFFFu, *abort == 0 && mbar_wait(mask_ready, 0, abort)) && *abort == 0;
-        if (ok) {
-            seq.begin(2);
-            while (ok && seq.next(&item, &centre)) ok = process(item, centre);
-        }
-        if (!ok) *abort = 1;
+        if (!boundary_done) boundary();
         if (live) {
             p.cand_count[r] = (ok && good) ? count : kNone;
-            p.final_t[r] = T;
+            p.final_t[r] = (ok && good) ? T : INFINITY;
         }
     }
     tc_fence_before();
@@ -511,7 +561,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     if (*abort && threadIdx.x == 0) atomicExch(p.error, 1);
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, kTmemCols);
+        tmem_dealloc(tmem, kCols);
     }
 }
 
@@ -541,6 +591,8 @@ struct RescoreArgs {
     float* out_dist;
     uint32_t* retry;
     uint32_t* retry_count;
+    float* retry_r2;          // per query index: the radius its plain search may use
+    float inv_s2;             // 1 / s^2
     DevCounters* counters;
 };
 
@@ -580,6 +632,10 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
     const uint32_t cnt = a.cand_count[r];
     if (cnt > a.cap) {
         if (lane == 0) {
+            // The plain search of this query may stop at the filter's final k-th upper bound:
+            // at least k points lie within it, so the answer is unchanged.
+            const float user = a.radii ? fminf(a.radii[qi], a.max_d2) : a.max_d2;
+            a.retry_r2[qi] = fminf(user, __fmul_ru(a.final_t[r], a.inv_s2));
             a.retry[atomicAdd(a.retry_count, 1u)] = qi;
             if (a.counters) atomicAdd(&a.counters->fallback, 1ull);
         }
@@ -644,6 +700,125 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
     if (a.counters) {
         for (int o = 16; o; o >>= 1) scored += __shfl_xor_sync(0xFFFFFFFFu, scored, o);
         if (lane == 0) atomicAdd(&a.counters->nodes, static_cast<unsigned long long>(scored));
+    }
+}
+
+// Exhaustive search for the queries the filter could not settle (listed in `retry`, count on the
+// device), split over kExhChunks blocks per query: each block scans its share of the point rows
+// with the reference's sequential FP32 distance, appends keys below the query's radius to a shared
+// buffer that is sorted and trimmed to the k smallest whenever it fills (the radius then tightens
+// to the k-th key), and writes its k smallest; a second kernel merges the chunks per query.
+constexpr uint32_t kExhThreads = 256;
+constexpr uint32_t kExhBuf = 2048;
+constexpr uint32_t kExhRound = 4;    // points per thread between buffer checks
+constexpr uint32_t kExhChunks = 8;   // blocks per query
+
+__device__ __forceinline__ void block_bitonic(uint64_t* buf, uint32_t n) {
+    for (uint32_t size = 2; size <= n; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t i = threadIdx.x; i < n / 2; i += blockDim.x) {
+                const uint32_t lo = 2 * stride * (i / stride) + (i % stride);
+                const uint32_t hi = lo + stride;
+                const bool up = (lo & size) == 0;
+                const uint64_t x = buf[lo], y = buf[hi];
+                if ((x > y) == up) {
+                    buf[lo] = y;
+                    buf[hi] = x;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Sorts buf[0, *fill) (padding to a power of two), keeps the k smallest and lowers *limit below
+// the k-th key.  Called by the whole block.
+__device__ __forceinline__ void block_trim(uint64_t* buf, uint32_t* fill, uint64_t* limit, uint32_t k) {
+    uint32_t n2 = 1;
+    while (n2 < *fill) n2 <<= 1;
+    for (uint32_t j = *fill + threadIdx.x; j < n2; j += blockDim.x) buf[j] = ~0ull;
+    __syncthreads();
+    block_bitonic(buf, n2);
+    if (threadIdx.x == 0) {
+        if (*fill >= k) *limit = min(*limit, buf[k - 1] + 1);  // keys above the k-th cannot enter
+        *fill = min(*fill, k);
+    }
+    __syncthreads();
+}
+
+template <int PS>
+__global__ void __launch_bounds__(kExhThreads) tc_exhaustive_kernel(const float* __restrict__ pts,
+                                                                    const uint32_t* __restrict__ ids,
+                                                                    const float* __restrict__ pnorm, uint32_t prows,
+                                                                    const float* __restrict__ queries, uint32_t dims,
+                                                                    uint32_t k, const uint32_t* __restrict__ retry,
+                                                                    const uint32_t* __restrict__ retry_count,
+                                                                    const float* __restrict__ retry_r2,
+                                                                    uint64_t* __restrict__ xkeys) {
+    __shared__ uint64_t buf[kExhBuf];
+    __shared__ uint32_t fill;
+    __shared__ uint64_t limit;
+    const uint32_t items = *retry_count * kExhChunks;
+    const uint32_t csize = (prows + kExhChunks - 1) / kExhChunks;
+    for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
+        const uint32_t e = item / kExhChunks, ch = item % kExhChunks;
+        const uint32_t qi = retry[e];
+        float qv[PS];
+#pragma unroll
+        for (int d = 0; d < PS; ++d) qv[d] = static_cast<uint32_t>(d) < dims ? queries[static_cast<size_t>(qi) * dims + d] : 0.0f;
+        if (threadIdx.x == 0) {
+            fill = 0;
+            limit = make_key(retry_r2[qi], -1);
+        }
+        __syncthreads();
+        const uint32_t lo = ch * csize, hi = min(prows, lo + csize);
+        for (uint32_t base = lo; base < hi; base += kExhThreads * kExhRound) {
+            const uint64_t lim = limit;
+#pragma unroll
+            for (uint32_t u = 0; u < kExhRound; ++u) {
+                const uint32_t pos = base + u * kExhThreads + threadIdx.x;
+                if (pos < hi && pnorm[pos] <= FLT_MAX) {
+                    const float d2 = dist2_vec4<PS>(qv, reinterpret_cast<const float4*>(pts + static_cast<size_t>(pos) * PS));
+                    const uint64_t key = make_key(d2, static_cast<int32_t>(ids[pos]));
+                    if (key < lim) buf[atomicAdd(&fill, 1u)] = key;
+                }
+            }
+            __syncthreads();
+            if (fill + kExhThreads * kExhRound > kExhBuf) block_trim(buf, &fill, &limit, k);
+        }
+        block_trim(buf, &fill, &limit, k);
+        uint64_t* out = xkeys + (static_cast<size_t>(e) * kExhChunks + ch) * k;
+        for (uint32_t j = threadIdx.x; j < k; j += blockDim.x) out[j] = j < fill ? buf[j] : ~0ull;
+        __syncthreads();
+    }
+}
+
+// Merges the kExhChunks partial lists of each retried query and writes its row.
+__global__ void __launch_bounds__(kExhThreads) tc_exhaustive_merge_kernel(uint32_t k, const uint32_t* __restrict__ retry,
+                                                                          const uint32_t* __restrict__ retry_count,
+                                                                          const float* __restrict__ retry_r2,
+                                                                          const uint64_t* __restrict__ xkeys,
+                                                                          int32_t* __restrict__ out_idx,
+                                                                          float* __restrict__ out_dist) {
+    __shared__ uint64_t buf[kExhChunks * kMaxK];
+    const uint32_t nretry = *retry_count;
+    const uint32_t m = kExhChunks * k;
+    uint32_t n2 = 1;
+    while (n2 < m) n2 <<= 1;
+    for (uint32_t e = blockIdx.x; e < nretry; e += gridDim.x) {
+        const uint32_t qi = retry[e];
+        const float r2 = retry_r2[qi];
+        for (uint32_t j = threadIdx.x; j < n2; j += blockDim.x)
+            buf[j] = j < m ? xkeys[static_cast<size_t>(e) * m + j] : ~0ull;
+        __syncthreads();
+        block_bitonic(buf, n2);
+        const uint64_t limit = make_key(r2, -1);
+        for (uint32_t j = threadIdx.x; j < k; j += blockDim.x) {
+            const bool have = buf[j] < limit;
+            out_idx[static_cast<size_t>(qi) * k + j] = have ? key_index(buf[j]) : -1;
+            out_dist[static_cast<size_t>(qi) * k + j] = have ? key_dist(buf[j]) : r2;
+        }
+        __syncthreads();
     }
 }
 
@@ -998,14 +1173,22 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
 }
 
 size_t filter_smem(uint32_t H, uint32_t k) {
-    return 1024 + a_bytes(H) + 2 * b_bytes(H) + 2 * kRowData * sizeof(float) + kMaskWords * sizeof(uint32_t) +
-           static_cast<size_t>(k) * kTileM * 4 + 10 * 8 + 8;
+    return 1024 + a_bytes(H) + 2 * b_bytes(H) + 2 * kRowData * sizeof(float) + kMaskWords * sizeof(uint32_t) + 16 +
+           (kStage + static_cast<size_t>(k)) * kTileM * 4 + 10 * 8 + 8;
 }
 
 // The filter allocates all 512 TMEM columns, so a second resident block on the same SM would
 // wait inside tcgen05.alloc; asking for more than half the SM's shared memory keeps one block
 // per SM.
-size_t filter_launch_smem(uint32_t H, uint32_t k) { return std::max<size_t>(filter_smem(H, k), 120 * 1024); }
+// One accumulator (two blocks per SM) when two blocks' shared memory fits an SM.
+uint32_t accumulators(uint32_t H, uint32_t k) { return 2 * (filter_smem(H, k) + 1024) <= 228 * 1024 ? 1u : 2u; }
+
+// A block allocates ACC x 256 TMEM columns of the SM's 512, so more resident blocks than
+// 512 / (ACC x 256) would wait inside tcgen05.alloc: the shared memory asked for caps them at one
+// block per SM (two accumulators) or two (one accumulator).
+size_t filter_launch_smem(uint32_t H, uint32_t k) {
+    return std::max<size_t>(filter_smem(H, k), accumulators(H, k) == 2 ? 120 * 1024 : 80 * 1024);
+}
 
 uint32_t halves(uint32_t dims) { return dims <= 64 ? 1u : 2u; }
 
@@ -1335,7 +1518,8 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     KNN_TRY(ix->tc.ws.reserve(carve_bytes({nq * 4ull, nq * 4ull, nq * 4ull, nq * 4ull, radix_sort_temp_bytes(nq),
                                             qimg_bytes, qrows * 4ull, qtiles * 16ull,
                                             static_cast<size_t>(nq) * cap * 4, static_cast<size_t>(nq) * cap * 4,
-                                            nq * 4ull, nq * 4ull, nq * 4ull, nq * 4ull, 256})));
+                                            nq * 4ull, nq * 4ull, nq * 4ull, nq * 4ull, nq * 4ull,
+                                            static_cast<size_t>(nq) * kExhChunks * a.k * 8, 256})));
     Carver c(ix->tc.ws.ptr);
     uint32_t* k0 = c.take<uint32_t>(nq);
     uint32_t* v0 = c.take<uint32_t>(nq);
@@ -1351,6 +1535,8 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     float* final_t = c.take<float>(nq);
     uint32_t* retry = c.take<uint32_t>(nq);
     float* seed = c.take<float>(nq);
+    float* retry_r2 = c.take<float>(nq);
+    uint64_t* xkeys = c.take<uint64_t>(static_cast<size_t>(nq) * kExhChunks * a.k);
     uint32_t* small = c.take<uint32_t>(64);  // [0] retry count, [1] error flag
     KNN_TRY_CUDA(cudaMemsetAsync(small, 0, 64 * sizeof(uint32_t), s));
 
@@ -1402,7 +1588,9 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     p.counters = a.counters;
     p.error = reinterpret_cast<int*>(small + 1);
     const size_t smem = filter_launch_smem(H, a.k);
-    auto kern = H == 1 ? tc_filter_kernel<1> : tc_filter_kernel<2>;
+    const uint32_t acc = accumulators(H, a.k);
+    auto kern = H == 1 ? (acc == 1 ? tc_filter_kernel<1, 1> : tc_filter_kernel<1, 2>)
+                       : (acc == 1 ? tc_filter_kernel<2, 1> : tc_filter_kernel<2, 2>);
     KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));
     kern<<<qtiles, kThreads, smem, s>>>(p);
@@ -1433,6 +1621,8 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     ra.out_dist = a.out_dist;
     ra.retry = retry;
     ra.retry_count = small;
+    ra.retry_r2 = retry_r2;
+    ra.inv_s2 = 1.0f / p.s2;
     ra.counters = a.counters;
     switch (T.ps) {
         case 4: KNN_TRY(rescore<4>(ra, nq, s)); break;
@@ -1443,11 +1633,24 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
         default: KNN_TRY(rescore<128>(ra, nq, s)); break;
     }
     // Queries whose candidates overflowed, that the 16-bit format could not hold, or whose filter
-    // block gave up, take the plain search of the index.
-    QueryArgs again = a;
-    again.order = retry;
-    again.count_dev = small;
-    return query_structure(ix, again, plain, s);
+    // block gave up: exhaustive search over the layout, one block each, within the radius the
+    // filter proved (at least k points lie inside it, so the answer is unchanged).
+    const uint32_t eg = 4u * static_cast<uint32_t>(sm_count());
+#define KNN_EXH(P_)                                                                                                \
+    case P_:                                                                                                       \
+        tc_exhaustive_kernel<P_><<<eg, kExhThreads, 0, s>>>(T.pts.as<float>(), T.ids.as<uint32_t>(),              \
+                                                             T.norm.as<float>(), T.ptiles * kTileN, a.queries,       \
+                                                             ix->dims, a.k, retry, small, retry_r2, xkeys);          \
+        break;
+    switch (T.ps) {
+        KNN_EXH(4) KNN_EXH(8) KNN_EXH(16) KNN_EXH(32) KNN_EXH(64)
+        default: KNN_EXH(128)
+    }
+#undef KNN_EXH
+    KNN_LAUNCHED();
+    tc_exhaustive_merge_kernel<<<eg, kExhThreads, 0, s>>>(a.k, retry, small, retry_r2, xkeys, a.out_idx, a.out_dist);
+    KNN_LAUNCHED();
+    return KNN_OK;
 }
 
 int tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* bad) {
