@@ -382,7 +382,8 @@ def run_c5(args, world, rank, local):
         "exact_match": {"chosen": rows_ok / rows, "plain": plain_ok / rows, "sample_queries": rows},
         "plain": {"value": plain_qps, "ms_per_step": plain_ms / args.steps,
                   "form": "one batchKnn per set with the reference benchmarks' template choices"},
-        "chosen": {"form": "one CUDA-graph launch, one persistent kernel per (tree, dims, k) class, autotuned",
+        "chosen": {"form": "one CUDA-graph launch: a persistent kernel per (tree, dims, k) class, or the "
+                           "tensor-core filter for classes of dims >= 16 where it times faster; autotuned",
                    "kernels_per_run": kernels_per_run, "speedup_vs_plain": value / plain_qps},
         "e2e": {"value": world * total_q * args.steps / e2e_s, "unit": "queries/s",
                 "h2d_bytes_per_step": int(sum(w.queries.nbytes for w in sets)),

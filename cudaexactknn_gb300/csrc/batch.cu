@@ -9,7 +9,9 @@
 // class are first sorted together by (set, leaf they descend to) for locality.  The classes are
 // the parallel branches of one captured CUDA graph, replayed with one cudaGraphLaunch per run.
 // Plans (leaf bucket size, block size, per-thread or warp-coherent traversal) come from the
-// autotuner, run on each class's largest set.
+// autotuner, run on each class's largest set; with autotuning, a class of dims >= 16 whose largest
+// set answers faster through the tensor-core filter runs its items through the filter instead, one
+// after another on a branch of their own.
 
 #include <algorithm>
 #include <cstring>
@@ -35,6 +37,7 @@ void kd_batch_set_fill(void*, const knn_index*, const QueryArgs&, const QueryPla
 void ball_batch_set_fill(void*, const knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, uint32_t,
                          uint32_t, uint32_t);
 int tune_plan(knn_index* ix, const QueryArgs& a, cudaStream_t s, QueryPlan* out);
+int query_structure(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 
 namespace {
 
@@ -71,6 +74,7 @@ struct knn_batch {
         uint32_t *counter = nullptr, *keys = nullptr, *vals = nullptr, *keys_alt = nullptr, *vals_alt = nullptr;
         void* sort_temp = nullptr;
         const uint32_t* order = nullptr;
+        bool tc = false;  // items run one by one through the tensor-core filter instead
     };
     std::vector<knn_batch_item> items;
     std::deque<Class> classes;  // stable addresses (the device buffers are not movable)
@@ -103,6 +107,32 @@ int enqueue_class(knn_batch::Class& c, cudaStream_t s) {
     KNN_TRY_CUDA(cudaMemsetAsync(c.counter, 0, sizeof(uint32_t), s));
     return knn::batch_launch(c.structure, c.dp, c.sets.ptr, static_cast<uint32_t>(c.items.size()), c.total_queries,
                              c.total_blocks, c.kmax, c.plan.warp, c.plan.block, c.counter, c.keys, c.vals, false, s);
+}
+
+knn::QueryArgs item_args(const knn_batch_item& it) {
+    return knn::QueryArgs{it.d_queries, it.count, it.max_distance2, nullptr, it.k, it.d_indexes, it.d_distances, nullptr};
+}
+
+// Best of two timed runs of one query on `s` (the run before them warms caches and workspaces).
+template <class F>
+int time_query(F&& run, cudaStream_t s, float* ms) {
+    cudaEvent_t e0, e1;
+    KNN_TRY_CUDA(cudaEventCreate(&e0));
+    KNN_TRY_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int rc = KNN_OK;
+    for (int rep = 0; rep < 3 && rc == KNN_OK; ++rep) {
+        cudaEventRecord(e0, s);
+        rc = run();
+        cudaEventRecord(e1, s);
+        if (rc == KNN_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(KNN_ERR_CUDA, "event");
+        float v = 0.0f;
+        if (rc == KNN_OK && rep > 0 && cudaEventElapsedTime(&v, e0, e1) == cudaSuccess) best = std::min(best, v);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = best;
+    return rc;
 }
 
 int check_item(const knn_batch_item& it) {
@@ -154,9 +184,35 @@ int knn_batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags
         c.plan.block = 128;
         if (flags & KNN_QF_AUTOTUNE) {
             const auto& it = items[largest];
-            knn::QueryArgs a{it.d_queries, it.count, it.max_distance2, nullptr, it.k, it.d_indexes, it.d_distances, nullptr};
+            const knn::QueryArgs a = item_args(it);
             if ((rc = knn::tune_plan(it.index, a, s, &c.plan)) != KNN_OK) break;
             c.plan.heap = c.plan.sh_nn = c.plan.sh_stack = false;  // the batch kernels keep tracker and stack in registers
+            // dims >= 16: the tensor-core filter instead, when it beats the tuned search on the
+            // class's largest set.
+            bool tc_ok = it.index->dims >= 16;
+            for (uint32_t i : c.items) tc_ok = tc_ok && knn::tc_supported(items[i].index->dims, items[i].k);
+            if (tc_ok) {
+                knn::QueryPlan tp;
+                tp.bf16 = true;
+                float t_tc = 0.0f, t_tree = 0.0f;
+                if ((rc = time_query([&] { return knn::bf_tc_query(it.index, a, tp, s); }, s, &t_tc)) != KNN_OK) break;
+                if ((rc = time_query([&] { return knn::query_structure(it.index, a, c.plan, s); }, s, &t_tree)) != KNN_OK)
+                    break;
+                c.tc = t_tc < t_tree;
+            }
+        }
+        if (c.tc) {
+            // Prepare each index's filter layout and workspace now (capture cannot allocate).
+            knn::QueryPlan tp;
+            tp.bf16 = true;
+            for (uint32_t i : c.items)
+                if ((rc = knn::bf_tc_query(items[i].index, item_args(items[i]), tp, s)) != KNN_OK) break;
+            if (rc != KNN_OK) break;
+            if (cudaStreamSynchronize(s) != cudaSuccess) {
+                rc = fail(KNN_ERR_CUDA, "stream synchronize");
+                break;
+            }
+            continue;
         }
         const uint32_t block = c.plan.block;
         uint32_t first_block = 0;
@@ -216,7 +272,7 @@ int knn_batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags
                                                                                    : fail(KNN_ERR_CUDA, "stream create");
         if (rc == KNN_OK) {
             b->streams.push_back(cap);
-            for (size_t i = 0; i < b->classes.size() && rc == KNN_OK; ++i) {
+            for (size_t i = 0; i <= b->classes.size() && rc == KNN_OK; ++i) {  // one stream per class, one for the filter
                 cudaStream_t cs = nullptr;
                 cudaEvent_t ev = nullptr;
                 if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess ||
@@ -233,13 +289,31 @@ int knn_batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags
                 rc = fail(KNN_ERR_CUDA, "graph capture could not start");
             if (rc == KNN_OK) {
                 int erc = cudaEventRecord(fork, cap) == cudaSuccess ? KNN_OK : fail(KNN_ERR_CUDA, "record");
-                for (size_t i = 0; i < b->classes.size() && erc == KNN_OK; ++i) {
+                // Filter classes share one branch, item after item: items of one index share its
+                // filter workspace.
+                const size_t nc = b->classes.size();
+                cudaStream_t tcs = b->streams[1 + nc];
+
+                if (erc == KNN_OK && cudaStreamWaitEvent(tcs, fork, 0) != cudaSuccess) erc = fail(KNN_ERR_CUDA, "fork");
+                for (size_t i = 0; i < nc && erc == KNN_OK; ++i) {
+                    auto& c = b->classes[i];
+                    if (c.tc) {
+                        knn::QueryPlan tp;
+                        tp.bf16 = true;
+                        for (uint32_t j : c.items)
+                            if (erc == KNN_OK) erc = knn::bf_tc_query(items[j].index, item_args(items[j]), tp, tcs);
+
+                        continue;
+                    }
                     cudaStream_t cs = b->streams[1 + i];
                     if (cudaStreamWaitEvent(cs, fork, 0) != cudaSuccess) erc = fail(KNN_ERR_CUDA, "fork");
-                    if (erc == KNN_OK) erc = enqueue_class(b->classes[i], cs);
+                    if (erc == KNN_OK) erc = enqueue_class(c, cs);
                     if (erc == KNN_OK && cudaEventRecord(b->events[i], cs) != cudaSuccess) erc = fail(KNN_ERR_CUDA, "join record");
                     if (erc == KNN_OK && cudaStreamWaitEvent(cap, b->events[i], 0) != cudaSuccess) erc = fail(KNN_ERR_CUDA, "join");
                 }
+                if (erc == KNN_OK && cudaEventRecord(b->events[nc], tcs) != cudaSuccess) erc = fail(KNN_ERR_CUDA, "join record");
+                if (erc == KNN_OK && cudaStreamWaitEvent(cap, b->events[nc], 0) != cudaSuccess) erc = fail(KNN_ERR_CUDA, "join");
+
                 cudaGraph_t g = nullptr;
                 const cudaError_t ee = cudaStreamEndCapture(cap, &g);
                 if (erc == KNN_OK && ee != cudaSuccess) erc = knn::cuda_fail(ee, "cudaStreamEndCapture", __FILE__, __LINE__);
