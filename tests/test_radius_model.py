@@ -101,3 +101,33 @@ def test_untrained_index_refuses_learned_radius():
     with pytest.raises(KnnError) as e:
         gu.run(ix, W.uniform(rng, 10, 3), 4, flags=_lib.QF_LEARNED_RADIUS)
     assert e.value.status == _lib.ERR_NOT_TRAINED
+
+
+@pytest.mark.parametrize("structure,d,k", [("kd", 3, 16), ("ball", 16, 32)])
+def test_learned_radius_gains_over_the_unseeded_search(structure, d, k):
+    """What the trained network buys: the seeded search visits fewer tree nodes and points than
+    the same search without a seed, and answers the same rows."""
+    from cudaexactknn_gb300 import _lib, knn
+    rng = np.random.default_rng(7 + d)
+    if d == 16:
+        pts, basis = W.subspace(rng, 200000, 16, 4, 0.05)
+        qs, _ = W.subspace(rng, 20000, 16, 4, 0.05, basis)
+        train, _ = W.subspace(rng, 16384, 16, 4, 0.05, basis)
+    else:
+        pts, centres = W.mixture(rng, 400000, d, 64, 0.01)
+        qs, _ = W.mixture(rng, 20000, d, 64, 0.01, centres)
+        train, _ = W.mixture(rng, 16384, d, 64, 0.01, centres)
+    ix = gu.make_index(structure, pts)
+    ix.train_radius_model(gu.to_dev(train), k, steps=1500)
+    q_plain = knn.Query(gu.to_dev(qs), len(qs), float("inf"))
+    q_seed = knn.Query(gu.to_dev(qs), len(qs), float("inf"))
+    plain = ix.stats(q_plain, k)
+    seeded = ix.stats(q_seed, k, flags=_lib.QF_LEARNED_RADIUS)
+    np.testing.assert_array_equal(q_plain.r_indexes.cpu().numpy(), q_seed.r_indexes.cpu().numpy())
+    np.testing.assert_array_equal(q_plain.r_distances.cpu().numpy(), q_seed.r_distances.cpu().numpy())
+    assert seeded.fallback_queries < len(qs) // 10
+    print(f"{structure}: nodes {seeded.nodes_visited / plain.nodes_visited:.3f}, "
+          f"points {seeded.points_scanned / plain.points_scanned:.3f} of the unseeded search, "
+          f"fallback {seeded.fallback_queries} of {len(qs)}")
+    assert seeded.nodes_visited < plain.nodes_visited, (seeded.nodes_visited, plain.nodes_visited)
+    assert seeded.points_scanned < plain.points_scanned, (seeded.points_scanned, plain.points_scanned)
