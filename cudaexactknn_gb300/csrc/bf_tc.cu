@@ -656,25 +656,39 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
     const uint32_t* c = a.cand + static_cast<size_t>(r) * a.cap;
     const float* cv = a.cand_v + static_cast<size_t>(r) * a.cap;
     uint32_t m = 0, scored = 0;
-    for (uint32_t i0 = 0; i0 < cnt; i0 += 32) {
-        const uint32_t i = i0 + lane;
-        uint64_t key = ~0ull;
-        if (i < cnt) {
-            const uint32_t pos = c[i];
-            const float pm = __ldg(a.pmax + pos / kTileN);
-            const float E = __fadd_ru(__fmaf_ru(c1q, pm, __fmul_ru(b.c3, __fadd_ru(qup, pm))), b.c4);
-            // Lower bound of s^2 times the pair's float distance.
-            const float lo = __fsub_rd(__fmaf_rd(-2.0f, cv[i], __fmul_rd(one_m_gn, __fadd_rd(nq, __ldg(a.pnorm + pos)))),
-                                       __fmul_ru(2.0f, E));
-            if (!(__fmul_rd(__fsub_rd(lo, b.c4), one_m_g) > tfin)) {
-                ++scored;
-                const float d2 = dist2_vec4<PS>(qv, reinterpret_cast<const float4*>(a.pts + static_cast<size_t>(pos) * PS));
-                key = make_key(d2, static_cast<int32_t>(a.ids[pos]));
-            }
-        }
+    // Whether candidate i must be rescored: its GEMM lower bound does not exceed T'.
+    auto needed = [&](uint32_t i, uint32_t* pos) {
+        if (i >= cnt) return false;
+        *pos = c[i];
+        const float pm = __ldg(a.pmax + *pos / kTileN);
+        const float E = __fadd_ru(__fmaf_ru(c1q, pm, __fmul_ru(b.c3, __fadd_ru(qup, pm))), b.c4);
+        // Lower bound of s^2 times the pair's float distance.
+        const float lo = __fsub_rd(__fmaf_rd(-2.0f, cv[i], __fmul_rd(one_m_gn, __fadd_rd(nq, __ldg(a.pnorm + *pos)))),
+                                   __fmul_ru(2.0f, E));
+        return !(__fmul_rd(__fsub_rd(lo, b.c4), one_m_g) > tfin);
+    };
+    auto append = [&](uint64_t key) {
         const bool take = key < limit;
         const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, take);
-        if (m + 32 > kRescoreBuf) {
+        if (take) buf[m + __popc(ballot & ((1u << lane) - 1u))] = key;
+        m += __popc(ballot);
+        __syncwarp();
+    };
+    // Two candidates per lane per step, their distance chains interleaved.
+    for (uint32_t i0 = 0; i0 < cnt; i0 += 64) {
+        uint32_t pa = 0, pb = 0;
+        const bool na = needed(i0 + lane, &pa), nb = needed(i0 + 32 + lane, &pb);
+        uint64_t ka = ~0ull, kb = ~0ull;
+        if (na || nb) {
+            const float4* ra = reinterpret_cast<const float4*>(a.pts + static_cast<size_t>(na ? pa : pb) * PS);
+            const float4* rb = reinterpret_cast<const float4*>(a.pts + static_cast<size_t>(nb ? pb : pa) * PS);
+            float da, db;
+            dist2_vec4_pair<PS>(qv, ra, rb, &da, &db);
+            if (na) ka = make_key(da, static_cast<int32_t>(a.ids[pa]));
+            if (nb) kb = make_key(db, static_cast<int32_t>(a.ids[pb]));
+            scored += (na ? 1u : 0u) + (nb ? 1u : 0u);
+        }
+        if (m + 64 > kRescoreBuf) {
             // Sort and keep the k smallest (the rest cannot be in the answer).
             uint32_t n2 = 1;
             while (n2 < m) n2 <<= 1;
@@ -683,9 +697,8 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
             warp_bitonic(buf, n2, lane);
             m = min(m, a.k);
         }
-        if (take) buf[m + __popc(ballot & ((1u << lane) - 1u))] = key;
-        m += __popc(ballot);
-        __syncwarp();
+        append(ka);
+        append(kb);
     }
     uint32_t n2 = 1;
     while (n2 < m) n2 <<= 1;

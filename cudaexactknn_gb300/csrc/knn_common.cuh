@@ -94,6 +94,36 @@ __device__ __forceinline__ float dist2_vec4(const float (&q)[DP], const float4* 
     return acc;
 }
 
+// Two rows at once: each distance is the same sequential fused sum as dist2_vec4 (identical
+// results), the two chains interleaved for instruction-level parallelism.
+template <int DP>
+__device__ __forceinline__ void dist2_vec4_pair(const float (&q)[DP], const float4* __restrict__ pa,
+                                                const float4* __restrict__ pb, float* da, float* db) {
+    static_assert(DP % 4 == 0, "vector path needs DP % 4 == 0");
+    float acc_a = 0.0f, acc_b = 0.0f;
+#pragma unroll
+    for (int v = 0; v < DP / 4; ++v) {
+        const float4 x = pa[v], y = pb[v];
+        float t = __fsub_rn(q[4 * v + 0], x.x), u = __fsub_rn(q[4 * v + 0], y.x);
+        acc_a = __fmaf_rn(t, t, acc_a);
+        acc_b = __fmaf_rn(u, u, acc_b);
+        t = __fsub_rn(q[4 * v + 1], x.y);
+        u = __fsub_rn(q[4 * v + 1], y.y);
+        acc_a = __fmaf_rn(t, t, acc_a);
+        acc_b = __fmaf_rn(u, u, acc_b);
+        t = __fsub_rn(q[4 * v + 2], x.z);
+        u = __fsub_rn(q[4 * v + 2], y.z);
+        acc_a = __fmaf_rn(t, t, acc_a);
+        acc_b = __fmaf_rn(u, u, acc_b);
+        t = __fsub_rn(q[4 * v + 3], x.w);
+        u = __fsub_rn(q[4 * v + 3], y.w);
+        acc_a = __fmaf_rn(t, t, acc_a);
+        acc_b = __fmaf_rn(u, u, acc_b);
+    }
+    *da = acc_a;
+    *db = acc_b;
+}
+
 // Select q[dim] from a register array without dynamic indexing (which would force the array
 // into local memory).
 template <int DP>
