@@ -80,6 +80,7 @@ constexpr uint32_t kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kCellPoints = 1024;
 constexpr uint32_t kMaxCells = 4096;
 constexpr uint32_t kMaskWords = kMaxCells / 32;
+constexpr uint32_t kBoxMaxDims = 32;  // the tree layout and its box test up to this many dims
 constexpr uint32_t kRowData = 2 * kTileN;  // floats of row data per tile: norms, then (centres) radii
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr uint32_t kStage = 16;               // accumulator values staged per thread for its hits
@@ -109,6 +110,10 @@ struct TcParams {
     const float* cmax;           // per centre tile: >= |c'|
     const uint32_t* cell_tile;   // [cells + 1] first point tile of each cell
     const uint32_t* qhome;       // per query tile: first tile, end tile, first cell, last cell
+    const float* box;            // tree layout: per cell [2][BD] scaled box (minima, maxima)
+    const float* queries;        // the caller's queries (for the box test)
+    uint32_t dims;
+    float scale;
     uint32_t cells, ctiles, nq, ksteps, idesc;
     Bounds b;
     float s2, max_d2;
@@ -209,7 +214,10 @@ __device__ __forceinline__ void epilogue_barrier() { asm volatile("bar.sync 1, %
 // ACC accumulators of kTileN TMEM columns: 2 lets the MMAs of the next tile run while the
 // epilogue drains this one (one block per SM); 1 leaves room for two blocks per SM, whose
 // epilogues then hide each other's latencies.
-template <uint32_t H, uint32_t ACC>
+// BD > 0 (tree layout): after the centre test, the kept cells are re-tested against the exact
+// distance from each query to each cell's axis-aligned box (the query's BD scaled coordinates in
+// registers).
+template <uint32_t H, uint32_t ACC, uint32_t BD>
 __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p) {
     constexpr uint32_t kCols = ACC * kTileN;
     extern __shared__ uint8_t smem_raw[];
@@ -377,6 +385,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         const float nq = live ? p.qnorm[r] : 0.0f;
         const bool good = live && nq <= FLT_MAX;  // NaN or +inf: not representable
         const Bounds& b = p.b;
+        float qb[BD > 0 ? BD : 1];
+#pragma unroll
+        for (uint32_t d = 0; d < (BD > 0 ? BD : 1); ++d)
+            qb[d] = (BD > 0 && good && d < p.dims) ? p.queries[static_cast<size_t>(qi) * p.dims + d] * p.scale : 0.0f;
         const float r2 = fminf(p.radii ? fminf(p.radii[qi], p.max_d2) : p.max_d2, p.seed[qi]);
         const float seed = good ? __fmul_ru(r2, p.s2) : 0.0f;
         BoundHeap heap{heap_base + row, p.k};
@@ -543,6 +555,36 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
             if (code == kEnd) break;
             if (code == kBoundary) {
                 release();
+                if constexpr (BD > 0) {
+                    // Box test of every cell the centre test kept: each query's exact distance to
+                    // the cell's box, lower-bounded with directed rounding; a cell stays when some
+                    // query may need it.
+                    epilogue_barrier();  // the centre test's mask is complete
+                    uint32_t* sNeed = reinterpret_cast<uint32_t*>(sStage);  // [kEpiWarps][kMaskWords]
+                    const uint32_t ew = warp - 2, mwords = (p.cells + 31) / 32;
+                    const float one_m_g = __fsub_rd(1.0f, b.g);
+                    for (uint32_t w = 0; w < mwords; ++w) {
+                        uint32_t bits = sMask[w], need = 0;
+                        while (bits) {
+                            const uint32_t bit = static_cast<uint32_t>(__ffs(bits) - 1);
+                            bits &= bits - 1u;
+                            if (!good) continue;
+                            const float* bx = p.box + static_cast<size_t>(w * 32 + bit) * 2 * BD;
+                            float acc = 0.0f;
+#pragma unroll
+                            for (uint32_t d = 0; d < BD; ++d) {
+                                const float gap = fmaxf(fmaxf(__fsub_rd(__ldg(bx + d), qb[d]), __fsub_rd(qb[d], __ldg(bx + BD + d))), 0.0f);
+                                acc = __fmaf_rd(gap, gap, acc);
+                            }
+                            if (!(__fsub_rd(__fmul_rd(acc, one_m_g), b.c4) > T)) need |= 1u << bit;
+                        }
+                        need = __reduce_or_sync(0xFFFFFFFFu, need);
+                        if (lane == 0) sNeed[ew * kMaskWords + w] = need;
+                    }
+                    epilogue_barrier();
+                    for (uint32_t w = threadIdx.x - 64; w < mwords; w += kEpiWarps * 32)
+                        sMask[w] &= sNeed[w] | sNeed[kMaskWords + w] | sNeed[2 * kMaskWords + w] | sNeed[3 * kMaskWords + w];
+                }
                 boundary();
                 continue;
             }
@@ -1067,6 +1109,172 @@ __global__ void tc_cdata_kernel(const float* __restrict__ cnorm, const float* __
     cdata[static_cast<size_t>(t) * kRowData + kTileN + j] = i < cells ? radius[i] : 0.0f;
 }
 
+// ---- tree layout (dims <= kBoxMaxDims): a tile-aligned partition tree --------------------------
+// Every node of m points covering t = ceil(m / 256) tiles sends its first ceil(t/2) * 256 points,
+// in the order of their coordinate along the node's widest dimension, to its left child; nodes of
+// one tile are leaves (cells).  The leaves are axis-aligned, compact tiles of 256 points (the last
+// one possibly partial), and the shape depends on n alone.
+
+__device__ __forceinline__ uint32_t order_key(float x) {
+    const uint32_t u = __float_as_uint(x);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float order_val(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+// Segment of each position: the last segment start <= i (starts ascending, starts[0] = 0).
+__global__ void kp_segment_kernel(const uint32_t* __restrict__ starts, uint32_t nseg, uint32_t n,
+                                  uint32_t* __restrict__ seg_of) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t lo = 0, hi = nseg;  // starts[lo] <= i < starts[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (starts[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    seg_of[i] = lo;
+}
+
+// Per split segment and dimension, the range of its points' coordinates (orderable keys).
+__global__ void kp_range_kernel(const float* __restrict__ src, uint32_t stride, uint32_t dims,
+                                const uint32_t* __restrict__ order, const uint32_t* __restrict__ seg_of,
+                                const uint8_t* __restrict__ split, uint32_t n, uint32_t* __restrict__ range) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t sg = seg_of[i];
+    if (!split[sg]) return;
+    const float* x = src + static_cast<size_t>(order[i]) * stride;
+    for (uint32_t d = 0; d < dims; ++d) {
+        const uint32_t key = order_key(x[d]);
+        atomicMin(range + (static_cast<size_t>(sg) * dims + d) * 2, key);
+        atomicMax(range + (static_cast<size_t>(sg) * dims + d) * 2 + 1, key);
+    }
+}
+
+// Widest dimension of each split segment (lowest on ties).
+__global__ void kp_dim_kernel(const uint32_t* __restrict__ range, const uint8_t* __restrict__ split, uint32_t nseg,
+                              uint32_t dims, uint32_t* __restrict__ seg_dim) {
+    const uint32_t sg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sg >= nseg || !split[sg]) return;
+    uint32_t best = 0;
+    float width = -1.0f;
+    for (uint32_t d = 0; d < dims; ++d) {
+        const float w = order_val(range[(static_cast<size_t>(sg) * dims + d) * 2 + 1]) -
+                        order_val(range[(static_cast<size_t>(sg) * dims + d) * 2]);
+        if (w > width) {
+            width = w;
+            best = d;
+        }
+    }
+    seg_dim[sg] = best;
+}
+
+__global__ void kp_key_kernel(const float* __restrict__ src, uint32_t stride, const uint32_t* __restrict__ order,
+                              const uint32_t* __restrict__ seg_of, const uint8_t* __restrict__ split,
+                              const uint32_t* __restrict__ seg_dim, uint32_t n, uint32_t* __restrict__ keys,
+                              uint32_t* __restrict__ vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t sg = seg_of[i];
+    keys[i] = split[sg] ? order_key(src[static_cast<size_t>(order[i]) * stride + seg_dim[sg]]) : 0u;
+    vals[i] = i;
+}
+
+__global__ void kp_segkey_kernel(const uint32_t* __restrict__ seg_of, const uint32_t* __restrict__ vals, uint32_t n,
+                                 uint32_t* __restrict__ keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) keys[i] = seg_of[vals[i]];
+}
+
+__global__ void kp_gather_kernel(const uint32_t* __restrict__ order, const uint32_t* __restrict__ vals, uint32_t n,
+                                 uint32_t* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = order[vals[i]];
+}
+
+// Split record of each split segment: its dimension and the coordinate of its last left point.
+__global__ void kp_node_kernel(const float* __restrict__ src, uint32_t stride, const uint32_t* __restrict__ order,
+                               const uint32_t* __restrict__ starts, const uint32_t* __restrict__ left,
+                               const uint32_t* __restrict__ node, const uint8_t* __restrict__ split,
+                               const uint32_t* __restrict__ seg_dim, uint32_t nseg, int32_t* __restrict__ node_dim,
+                               float* __restrict__ node_val) {
+    const uint32_t sg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sg >= nseg || !split[sg]) return;
+    node_dim[node[sg]] = static_cast<int32_t>(seg_dim[sg]);
+    node_val[node[sg]] = src[static_cast<size_t>(order[starts[sg] + left[sg] - 1]) * stride + seg_dim[sg]];
+}
+
+// Axis-aligned box of each cell's rows in scaled coordinates (exact: the scale is a power of two),
+// [cells][2][bd]: minima then maxima, zero past `dims`.
+__global__ void tc_box_kernel(const float* __restrict__ pts, uint32_t ps, uint32_t dims, float scale,
+                              const float* __restrict__ norm, const uint32_t* __restrict__ cell_tile, uint32_t cells,
+                              uint32_t bd, float* __restrict__ box) {
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x % 32;
+    if (c >= cells || lane >= bd) return;
+    float lo = INFINITY, hi = -INFINITY;
+    for (uint32_t r = cell_tile[c] * kTileN; r < cell_tile[c + 1] * kTileN; ++r) {
+        if (!(norm[r] <= FLT_MAX) || lane >= dims) continue;
+        const float x = pts[static_cast<size_t>(r) * ps + lane] * scale;
+        lo = fminf(lo, x);
+        hi = fmaxf(hi, x);
+    }
+    if (lane >= dims || lo > hi) lo = hi = 0.0f;
+    box[static_cast<size_t>(c) * 2 * bd + lane] = lo;
+    box[static_cast<size_t>(c) * 2 * bd + bd + lane] = hi;
+}
+
+// Leaf cell each query descends to; rows past the live count get key `cells`.  vals = the
+// query index; seed[query] = an upper bound on its k-th float distance from its own cell's ball
+// (centre c', radius R, scaled): ((|q' - c'| + R)^2 (1 + g) + slack) / s^2, when the cell holds
+// >= k points, else +inf.
+template <int DP>
+__global__ void __launch_bounds__(128) kp_descend_kernel(const float* __restrict__ queries, uint32_t dims,
+                                                         uint32_t rows, const uint32_t* __restrict__ order,
+                                                         const uint32_t* __restrict__ live_count,
+                                                         const int32_t* __restrict__ node_dim,
+                                                         const float* __restrict__ node_val,
+                                                         const int32_t* __restrict__ node_leaf, uint32_t cells,
+                                                         const float* __restrict__ centre, uint32_t ps,
+                                                         const float* __restrict__ radius,
+                                                         const uint32_t* __restrict__ cell_start, uint32_t k,
+                                                         float scale, uint32_t* __restrict__ keys,
+                                                         uint32_t* __restrict__ vals, float* __restrict__ seed) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const bool live = r < (live_count ? *live_count : rows);
+    const uint32_t qi = live ? (order ? order[r] : r) : 0u;
+    uint32_t key = cells;
+    if (live) {
+        float q[DP];
+#pragma unroll
+        for (int d = 0; d < DP; ++d) q[d] = static_cast<uint32_t>(d) < dims ? queries[static_cast<size_t>(qi) * dims + d] : 0.0f;
+        uint32_t nd = 0;
+        for (int depth = 0; depth < 32 && node_leaf[nd] < 0; ++depth)
+            nd = pick<DP>(q, static_cast<uint32_t>(node_dim[nd])) <= node_val[nd] ? 2 * nd + 1 : 2 * nd + 2;
+        const uint32_t c = node_leaf[nd] >= 0 ? min(static_cast<uint32_t>(node_leaf[nd]), cells - 1) : 0u;
+        key = c;
+        float t = INFINITY;
+        if (cell_start[c + 1] - cell_start[c] >= k) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int d = 0; d < DP; ++d) {
+                const float e = __fsub_rn(q[d] * scale, centre[static_cast<size_t>(c) * ps + d]);
+                acc = __fmaf_rn(e, e, acc);
+            }
+            const float g = rel_margin(dims);
+            const float a = __fsqrt_ru(__fmul_ru(acc, __frcp_ru(__fsub_rd(1.0f, g))));  // >= exact |q' - c'|
+            const float u = __fadd_ru(a, radius[c]);
+            const float t_scaled = __fadd_ru(__fmul_ru(__fmul_ru(u, u), __fadd_ru(1.0f, g)), 0x1p-120f);
+            t = __fmul_ru(t_scaled, 1.0f / (scale * scale));
+        }
+        seed[qi] = t;
+    }
+    keys[r] = key;
+    vals[r] = qi;
+}
+
 // Squared float distances between all pairs of landmarks ([cells][cells]).
 __global__ void tc_pair_d2_kernel(const float* __restrict__ land, uint32_t ps, uint32_t dims, uint32_t cells,
                                   float* __restrict__ out) {
@@ -1244,6 +1452,26 @@ int launch_assign(uint32_t dp, const float* src, uint32_t stride, uint32_t dims,
     return KNN_OK;
 }
 
+int launch_descend(uint32_t dp, const float* queries, uint32_t dims, uint32_t rows, const uint32_t* order,
+                   const uint32_t* live_count, const knn_index::TensorCoreState& T, uint32_t k, uint32_t* keys,
+                   uint32_t* vals, float* seed, cudaStream_t s) {
+    const uint32_t grid = ceil_div(rows, 128);
+#define KNN_DESCEND(D_)                                                                                               \
+    case D_:                                                                                                          \
+        kp_descend_kernel<D_><<<grid, 128, 0, s>>>(queries, dims, rows, order, live_count, T.node_dim.as<int32_t>(),  \
+                                                    T.node_val.as<float>(), T.node_leaf.as<int32_t>(), T.cells,        \
+                                                    T.ccentre.as<float>(), T.ps, T.cradius.as<float>(),                \
+                                                    T.cell_start.as<uint32_t>(), k, T.scale, keys, vals, seed);        \
+        break;
+    switch (dp) {
+        KNN_DESCEND(1) KNN_DESCEND(2) KNN_DESCEND(3) KNN_DESCEND(4) KNN_DESCEND(8) KNN_DESCEND(16) KNN_DESCEND(32)
+        default: return fail(KNN_ERR_UNSUPPORTED, "tree layout beyond %u dims", kBoxMaxDims);
+    }
+#undef KNN_DESCEND
+    KNN_LAUNCHED();
+    return KNN_OK;
+}
+
 }  // namespace
 
 bool tc_supported(uint32_t dims, uint32_t k) {
@@ -1314,146 +1542,299 @@ int tc_prepare(knn_index* ix, cudaStream_t s) {
     T.scale = T.f16 ? std::ldexp(1.0f, e) : 1.0f;
     T.ps = ps;
 
-    // Landmarks: every (n/L)-th point; then, up to three times, a landmark at the farthest point
-    // of each cell whose farthest squared distance exceeds 4x the 25th percentile over cells (a
-    // cell holding two clusters is split); finally the landmarks in the order of a greedy
-    // nearest-neighbour chain, so that consecutive cells lie near each other.
-    std::vector<uint32_t> lrows;
-    {
-        const uint32_t L0 = std::max(1u, std::min(kMaxCells / 2, n / kCellPoints));
-        for (uint32_t j = 0; j < L0; ++j) lrows.push_back(static_cast<uint32_t>(static_cast<uint64_t>(j) * n / L0));
-    }
-    DevBuf sortb;
-    KNN_TRY(sortb.alloc(carve_bytes({n * 4ull, n * 4ull, n * 4ull, n * 4ull, radix_sort_temp_bytes(n), kMaxCells * 8ull,
-                                     kMaxCells * 4ull})));
-    Carver sc(sortb.ptr);
-    uint32_t* k0 = sc.take<uint32_t>(n);
-    uint32_t* v0 = sc.take<uint32_t>(n);
-    uint32_t* k1 = sc.take<uint32_t>(n);
-    uint32_t* v1 = sc.take<uint32_t>(n);
-    void* st = sc.take<uint8_t>(radix_sort_temp_bytes(n));
-    unsigned long long* far = sc.take<unsigned long long>(kMaxCells);
-    uint32_t* lr = sc.take<uint32_t>(kMaxCells);
-    KNN_TRY(T.land.alloc(static_cast<size_t>(kMaxCells) * ps * 4));
-    auto place_landmarks = [&]() -> int {
-        const uint32_t cells = static_cast<uint32_t>(lrows.size());
-        KNN_TRY_CUDA(cudaMemcpyAsync(lr, lrows.data(), cells * 4ull, cudaMemcpyHostToDevice, s));
-        tc_gather_rows_kernel<<<ceil_div(cells * ps, 256), 256, 0, s>>>(src, stride, dims, lr, cells, ps,
-                                                                       T.land.as<float>());
-        KNN_LAUNCHED();
-        KNN_TRY(launch_assign(ix->dp, src, stride, dims, n, nullptr, nullptr, T.land.as<float>(), ps, cells, k0, v0, s));
-        KNN_TRY_CUDA(cudaStreamSynchronize(s));  // lrows is reused
-        return KNN_OK;
-    };
-    for (int round = 0;; ++round) {
-        const uint32_t cells = static_cast<uint32_t>(lrows.size());
-        KNN_TRY(place_landmarks());
-        if (round == 3 || cells >= kMaxCells) break;
+    // Cells: the leaves of a partition tree at low dims (axis-aligned, tight boxes), landmark cells
+    // otherwise (boxes say little in many dims; the centre test does the work).
+    T.tree = dims <= kBoxMaxDims;
+    uint32_t cells = 0;
+    std::vector<uint32_t> cell_start, cell_tile;
+    DevBuf rowmap;
+    if (T.tree) {
+        {
+            struct Node {
+                uint32_t start = 0, size = 0, depth = 0;
+                int32_t leaf = -1;
+                bool used = false;
+            };
+            std::vector<Node> shape(1);
+            shape[0] = Node{0, n, 0, -1, true};
+            uint32_t max_depth = 0;
+            // Leaves of up to `lt` tiles, so that there are at most kMaxCells of them.
+            const uint32_t lt = std::max(1u, ceil_div(ceil_div(n, kTileN), kMaxCells));
+            for (std::vector<uint32_t> work{0}; !work.empty();) {
+                const uint32_t id = work.back();
+                work.pop_back();
+                const Node nd = shape[id];
+                const uint32_t t = ceil_div(nd.size, kTileN);
+                if (t <= lt) {
+                    shape[id].leaf = 0;  // numbered in position order below
+                    continue;
+                }
+                max_depth = std::max(max_depth, nd.depth);
+                const uint32_t left = (t + 1) / 2 * kTileN;
+                if (shape.size() < 2 * static_cast<size_t>(id) + 3) shape.resize(2 * static_cast<size_t>(id) + 3);
+                shape[2 * id + 1] = Node{nd.start, left, nd.depth + 1, -1, true};
+                shape[2 * id + 2] = Node{nd.start + left, nd.size - left, nd.depth + 1, -1, true};
+                work.push_back(2 * id + 1);
+                work.push_back(2 * id + 2);
+            }
+            const uint32_t nodes = static_cast<uint32_t>(shape.size());
+            std::vector<uint32_t> leaves;
+            for (uint32_t i = 0; i < nodes; ++i)
+                if (shape[i].used && shape[i].leaf >= 0) leaves.push_back(i);
+            std::sort(leaves.begin(), leaves.end(), [&](uint32_t x, uint32_t y) { return shape[x].start < shape[y].start; });
+            for (uint32_t c = 0; c < leaves.size(); ++c) shape[leaves[c]].leaf = static_cast<int32_t>(c);
+            KNN_TRY(T.node_dim.alloc(nodes * 4ull));
+            KNN_TRY(T.node_val.alloc(nodes * 4ull));
+            KNN_TRY(T.node_leaf.alloc(nodes * 4ull));
+            KNN_TRY_CUDA(cudaMemsetAsync(T.node_dim.ptr, 0, nodes * 4ull, s));
+            KNN_TRY_CUDA(cudaMemsetAsync(T.node_val.ptr, 0, nodes * 4ull, s));
+            std::vector<int32_t> leaf(nodes, 0);
+            for (uint32_t i = 0; i < nodes; ++i) leaf[i] = shape[i].used ? shape[i].leaf : 0;
+            KNN_TRY_CUDA(cudaMemcpyAsync(T.node_leaf.ptr, leaf.data(), nodes * 4ull, cudaMemcpyHostToDevice, s));
+            DevBuf tb;
+            KNN_TRY(tb.alloc(carve_bytes({n * 4ull, n * 4ull, n * 4ull, n * 4ull, n * 4ull, n * 4ull, n * 4ull,
+                                          radix_sort_temp_bytes(n), nodes * 4ull, nodes * 4ull, nodes * 4ull, nodes * 1ull,
+                                          nodes * 4ull, static_cast<size_t>(nodes) * dims * 8})));
+            Carver tc_(tb.ptr);
+            uint32_t* order = tc_.take<uint32_t>(n);
+            uint32_t* order_alt = tc_.take<uint32_t>(n);
+            uint32_t* seg_of = tc_.take<uint32_t>(n);
+            uint32_t* q0 = tc_.take<uint32_t>(n);
+            uint32_t* w0 = tc_.take<uint32_t>(n);
+            uint32_t* q1 = tc_.take<uint32_t>(n);
+            uint32_t* w1 = tc_.take<uint32_t>(n);
+            void* tst = tc_.take<uint8_t>(radix_sort_temp_bytes(n));
+            uint32_t* d_starts = tc_.take<uint32_t>(nodes);
+            uint32_t* d_left = tc_.take<uint32_t>(nodes);
+            uint32_t* d_node = tc_.take<uint32_t>(nodes);
+            uint8_t* d_split = tc_.take<uint8_t>(nodes);
+            uint32_t* seg_dim = tc_.take<uint32_t>(nodes);
+            uint32_t* range = tc_.take<uint32_t>(static_cast<size_t>(nodes) * dims * 2);
+            {
+                std::vector<uint32_t> iota(n);
+                std::iota(iota.begin(), iota.end(), 0u);
+                KNN_TRY_CUDA(cudaMemcpyAsync(order, iota.data(), n * 4ull, cudaMemcpyHostToDevice, s));
+                KNN_TRY_CUDA(cudaStreamSynchronize(s));
+            }
+            for (uint32_t depth = 0; leaves.size() > 1 && depth <= max_depth; ++depth) {
+                // Frontier in position order: the nodes of this depth and the shallower leaves.
+                std::vector<uint32_t> ids;
+                for (uint32_t i = 0; i < nodes; ++i)
+                    if (shape[i].used && (shape[i].depth == depth || (shape[i].leaf >= 0 && shape[i].depth < depth)))
+                        ids.push_back(i);
+                std::sort(ids.begin(), ids.end(), [&](uint32_t x, uint32_t y) { return shape[x].start < shape[y].start; });
+                const uint32_t nseg = static_cast<uint32_t>(ids.size());
+                std::vector<uint32_t> starts(nseg), left(nseg);
+                std::vector<uint8_t> split(nseg);
+                for (uint32_t j = 0; j < nseg; ++j) {
+                    const Node& nd = shape[ids[j]];
+                    starts[j] = nd.start;
+                    split[j] = nd.leaf < 0 && nd.depth == depth;
+                    left[j] = split[j] ? (ceil_div(nd.size, kTileN) + 1) / 2 * kTileN : 0u;
+                }
+                KNN_TRY_CUDA(cudaMemcpyAsync(d_starts, starts.data(), nseg * 4ull, cudaMemcpyHostToDevice, s));
+                KNN_TRY_CUDA(cudaMemcpyAsync(d_left, left.data(), nseg * 4ull, cudaMemcpyHostToDevice, s));
+                KNN_TRY_CUDA(cudaMemcpyAsync(d_node, ids.data(), nseg * 4ull, cudaMemcpyHostToDevice, s));
+                KNN_TRY_CUDA(cudaMemcpyAsync(d_split, split.data(), nseg, cudaMemcpyHostToDevice, s));
+                kp_segment_kernel<<<ceil_div(n, 256), 256, 0, s>>>(d_starts, nseg, n, seg_of);
+                KNN_LAUNCHED();
+                // Range per segment and dimension: minima start at all ones, maxima at zero.
+                std::vector<uint32_t> init(static_cast<size_t>(nseg) * dims * 2);
+                for (size_t e = 0; e < init.size(); ++e) init[e] = (e % 2 == 0) ? 0xFFFFFFFFu : 0u;
+                KNN_TRY_CUDA(cudaMemcpyAsync(range, init.data(), init.size() * 4, cudaMemcpyHostToDevice, s));
+                kp_range_kernel<<<ceil_div(n, 128), 128, 0, s>>>(src, stride, dims, order, seg_of, d_split, n, range);
+                KNN_LAUNCHED();
+                kp_dim_kernel<<<ceil_div(nseg, 128), 128, 0, s>>>(range, d_split, nseg, dims, seg_dim);
+                KNN_LAUNCHED();
+                // Positions by (segment, coordinate along its widest dimension): coordinate first,
+                // then segment (stable).
+                kp_key_kernel<<<ceil_div(n, 256), 256, 0, s>>>(src, stride, order, seg_of, d_split, seg_dim, n, q0, w0);
+                KNN_LAUNCHED();
+                bool alt = false;
+                KNN_TRY(radix_sort_pairs(q0, w0, q1, w1, n, 32, tst, s, &alt));
+                uint32_t* ka = alt ? q1 : q0;
+                uint32_t* va = alt ? w1 : w0;
+                uint32_t* kb = alt ? q0 : q1;
+                uint32_t* vb = alt ? w0 : w1;
+                kp_segkey_kernel<<<ceil_div(n, 256), 256, 0, s>>>(seg_of, va, n, ka);
+                KNN_LAUNCHED();
+                bool alt2 = false;
+                KNN_TRY(radix_sort_pairs(ka, va, kb, vb, n, static_cast<int>(log2_ceil(nseg + 1)), tst, s, &alt2));
+                kp_gather_kernel<<<ceil_div(n, 256), 256, 0, s>>>(order, alt2 ? vb : va, n, order_alt);
+                KNN_LAUNCHED();
+                std::swap(order, order_alt);
+                kp_node_kernel<<<ceil_div(nseg, 128), 128, 0, s>>>(src, stride, order, d_starts, d_left, d_node, d_split,
+                                                                   seg_dim, nseg, T.node_dim.as<int32_t>(),
+                                                                   T.node_val.as<float>());
+                KNN_LAUNCHED();
+                KNN_TRY_CUDA(cudaStreamSynchronize(s));  // the host vectors above are reused next level
+            }
+            cells = static_cast<uint32_t>(leaves.size());
+            cell_start.resize(cells + 1);
+            cell_tile.resize(cells + 1);
+            for (uint32_t c = 0; c < cells; ++c) {
+                cell_start[c] = shape[leaves[c]].start;
+                cell_tile[c] = shape[leaves[c]].start / kTileN;
+            }
+            cell_start[cells] = n;
+            cell_tile[cells] = ceil_div(n, kTileN);
+            KNN_TRY(T.cell_start.alloc((cells + 1) * 4ull));
+            KNN_TRY(T.cell_tile.alloc((cells + 1) * 4ull));
+            KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_start.ptr, cell_start.data(), (cells + 1) * 4ull, cudaMemcpyHostToDevice, s));
+            KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_tile.ptr, cell_tile.data(), (cells + 1) * 4ull, cudaMemcpyHostToDevice, s));
+            const uint32_t prows = cell_tile[cells] * kTileN;
+            KNN_TRY(rowmap.alloc(prows * 4ull));
+            KNN_TRY_CUDA(cudaMemsetAsync(rowmap.ptr, 0xFF, prows * 4ull, s));
+            KNN_TRY_CUDA(cudaMemcpyAsync(rowmap.ptr, order, n * 4ull, cudaMemcpyDeviceToDevice, s));
+            KNN_TRY_CUDA(cudaStreamSynchronize(s));
+        }
+
+    } else {
+        // Landmarks: every (n/L)-th point; then, up to three times, a landmark at the farthest point
+        // of each cell whose farthest squared distance exceeds 4x the 25th percentile over cells (a
+        // cell holding two clusters is split); finally the landmarks in the order of a greedy
+        // nearest-neighbour chain, so that consecutive cells lie near each other.
+        std::vector<uint32_t> lrows;
+        {
+            const uint32_t L0 = std::max(1u, std::min(kMaxCells / 2, n / kCellPoints));
+            for (uint32_t j = 0; j < L0; ++j) lrows.push_back(static_cast<uint32_t>(static_cast<uint64_t>(j) * n / L0));
+        }
+        DevBuf sortb;
+        KNN_TRY(sortb.alloc(carve_bytes({n * 4ull, n * 4ull, n * 4ull, n * 4ull, radix_sort_temp_bytes(n), kMaxCells * 8ull,
+                                         kMaxCells * 4ull})));
+        Carver sc(sortb.ptr);
+        uint32_t* k0 = sc.take<uint32_t>(n);
+        uint32_t* v0 = sc.take<uint32_t>(n);
+        uint32_t* k1 = sc.take<uint32_t>(n);
+        uint32_t* v1 = sc.take<uint32_t>(n);
+        void* st = sc.take<uint8_t>(radix_sort_temp_bytes(n));
+        unsigned long long* far = sc.take<unsigned long long>(kMaxCells);
+        uint32_t* lr = sc.take<uint32_t>(kMaxCells);
+        KNN_TRY(T.land.alloc(static_cast<size_t>(kMaxCells) * ps * 4));
+        auto place_landmarks = [&]() -> int {
+            const uint32_t cells = static_cast<uint32_t>(lrows.size());
+            KNN_TRY_CUDA(cudaMemcpyAsync(lr, lrows.data(), cells * 4ull, cudaMemcpyHostToDevice, s));
+            tc_gather_rows_kernel<<<ceil_div(cells * ps, 256), 256, 0, s>>>(src, stride, dims, lr, cells, ps,
+                                                                           T.land.as<float>());
+            KNN_LAUNCHED();
+            KNN_TRY(launch_assign(ix->dp, src, stride, dims, n, nullptr, nullptr, T.land.as<float>(), ps, cells, k0, v0, s));
+            KNN_TRY_CUDA(cudaStreamSynchronize(s));  // lrows is reused
+            return KNN_OK;
+        };
+        for (int round = 0;; ++round) {
+            const uint32_t cells = static_cast<uint32_t>(lrows.size());
+            KNN_TRY(place_landmarks());
+            if (round == 3 || cells >= kMaxCells) break;
+            KNN_TRY_CUDA(cudaMemsetAsync(far, 0, cells * 8ull, s));
+            tc_cell_far_kernel<<<ceil_div(n, 256), 256, 0, s>>>(src, stride, dims, k0, n, T.land.as<float>(), ps, far);
+            KNN_LAUNCHED();
+            std::vector<unsigned long long> hfar(cells);
+            KNN_TRY_CUDA(cudaMemcpyAsync(hfar.data(), far, cells * 8ull, cudaMemcpyDeviceToHost, s));
+            KNN_TRY_CUDA(cudaStreamSynchronize(s));
+            std::vector<float> d2;
+            for (auto f : hfar) {
+                float v;
+                const uint32_t bits = static_cast<uint32_t>(f >> 32);
+                std::memcpy(&v, &bits, 4);
+                if (f) d2.push_back(v);
+            }
+            if (d2.empty()) break;
+            std::vector<float> sorted = d2;
+            std::nth_element(sorted.begin(), sorted.begin() + sorted.size() / 4, sorted.end());
+            const float q25 = sorted[sorted.size() / 4];
+            uint32_t added = 0;
+            for (uint32_t c = 0; c < cells && lrows.size() < kMaxCells; ++c) {
+                if (!hfar[c]) continue;
+                float v;
+                const uint32_t bits = static_cast<uint32_t>(hfar[c] >> 32);
+                std::memcpy(&v, &bits, 4);
+                if (v > 4.0f * q25 && v > 0.0f) {
+                    lrows.push_back(static_cast<uint32_t>(hfar[c] & 0xFFFFFFFFu));
+                    ++added;
+                }
+            }
+            if (!added) break;
+        }
+        cells = static_cast<uint32_t>(lrows.size());
+        if (cells > 2) {
+            DevBuf pd;
+            KNN_TRY(pd.alloc(static_cast<size_t>(cells) * cells * 4));
+            tc_pair_d2_kernel<<<static_cast<uint32_t>((static_cast<uint64_t>(cells) * cells + 255) / 256), 256, 0, s>>>(
+                T.land.as<float>(), ps, dims, cells, pd.as<float>());
+            KNN_LAUNCHED();
+            std::vector<float> hd(static_cast<size_t>(cells) * cells);
+            KNN_TRY_CUDA(cudaMemcpyAsync(hd.data(), pd.ptr, hd.size() * 4, cudaMemcpyDeviceToHost, s));
+            KNN_TRY_CUDA(cudaStreamSynchronize(s));
+            std::vector<uint8_t> seen(cells, 0);
+            std::vector<uint32_t> chain{0};
+            seen[0] = 1;
+            for (uint32_t step = 1; step < cells; ++step) {
+                const float* row = hd.data() + static_cast<size_t>(chain.back()) * cells;
+                uint32_t best = kNone;
+                for (uint32_t j = 0; j < cells; ++j)
+                    if (!seen[j] && (best == kNone || row[j] < row[best])) best = j;
+                seen[best] = 1;
+                chain.push_back(best);
+            }
+            std::vector<uint32_t> reordered(cells);
+            for (uint32_t i = 0; i < cells; ++i) reordered[i] = lrows[chain[i]];
+            lrows.swap(reordered);
+            KNN_TRY(place_landmarks());
+        }
+
+        // Farthest squared distance from each final landmark to its cell's points (query seeds).
         KNN_TRY_CUDA(cudaMemsetAsync(far, 0, cells * 8ull, s));
         tc_cell_far_kernel<<<ceil_div(n, 256), 256, 0, s>>>(src, stride, dims, k0, n, T.land.as<float>(), ps, far);
         KNN_LAUNCHED();
-        std::vector<unsigned long long> hfar(cells);
-        KNN_TRY_CUDA(cudaMemcpyAsync(hfar.data(), far, cells * 8ull, cudaMemcpyDeviceToHost, s));
-        KNN_TRY_CUDA(cudaStreamSynchronize(s));
-        std::vector<float> d2;
-        for (auto f : hfar) {
-            float v;
-            const uint32_t bits = static_cast<uint32_t>(f >> 32);
-            std::memcpy(&v, &bits, 4);
-            if (f) d2.push_back(v);
-        }
-        if (d2.empty()) break;
-        std::vector<float> sorted = d2;
-        std::nth_element(sorted.begin(), sorted.begin() + sorted.size() / 4, sorted.end());
-        const float q25 = sorted[sorted.size() / 4];
-        uint32_t added = 0;
-        for (uint32_t c = 0; c < cells && lrows.size() < kMaxCells; ++c) {
-            if (!hfar[c]) continue;
-            float v;
-            const uint32_t bits = static_cast<uint32_t>(hfar[c] >> 32);
-            std::memcpy(&v, &bits, 4);
-            if (v > 4.0f * q25 && v > 0.0f) {
-                lrows.push_back(static_cast<uint32_t>(hfar[c] & 0xFFFFFFFFu));
-                ++added;
+        {
+            std::vector<unsigned long long> hfar(cells);
+            KNN_TRY_CUDA(cudaMemcpyAsync(hfar.data(), far, cells * 8ull, cudaMemcpyDeviceToHost, s));
+            KNN_TRY_CUDA(cudaStreamSynchronize(s));
+            std::vector<float> cf(cells);
+            for (uint32_t c = 0; c < cells; ++c) {
+                const uint32_t bits = static_cast<uint32_t>(hfar[c] >> 32);
+                std::memcpy(&cf[c], &bits, 4);
             }
+            KNN_TRY(T.cell_far.alloc(cells * 4ull));
+            KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_far.ptr, cf.data(), cells * 4ull, cudaMemcpyHostToDevice, s));
+            KNN_TRY_CUDA(cudaStreamSynchronize(s));
         }
-        if (!added) break;
-    }
-    const uint32_t cells = static_cast<uint32_t>(lrows.size());
-    T.cells = cells;
-    if (cells > 2) {
-        DevBuf pd;
-        KNN_TRY(pd.alloc(static_cast<size_t>(cells) * cells * 4));
-        tc_pair_d2_kernel<<<static_cast<uint32_t>((static_cast<uint64_t>(cells) * cells + 255) / 256), 256, 0, s>>>(
-            T.land.as<float>(), ps, dims, cells, pd.as<float>());
-        KNN_LAUNCHED();
-        std::vector<float> hd(static_cast<size_t>(cells) * cells);
-        KNN_TRY_CUDA(cudaMemcpyAsync(hd.data(), pd.ptr, hd.size() * 4, cudaMemcpyDeviceToHost, s));
-        KNN_TRY_CUDA(cudaStreamSynchronize(s));
-        std::vector<uint8_t> seen(cells, 0);
-        std::vector<uint32_t> chain{0};
-        seen[0] = 1;
-        for (uint32_t step = 1; step < cells; ++step) {
-            const float* row = hd.data() + static_cast<size_t>(chain.back()) * cells;
-            uint32_t best = kNone;
-            for (uint32_t j = 0; j < cells; ++j)
-                if (!seen[j] && (best == kNone || row[j] < row[best])) best = j;
-            seen[best] = 1;
-            chain.push_back(best);
-        }
-        std::vector<uint32_t> reordered(cells);
-        for (uint32_t i = 0; i < cells; ++i) reordered[i] = lrows[chain[i]];
-        lrows.swap(reordered);
-        KNN_TRY(place_landmarks());
-    }
 
-    // Farthest squared distance from each final landmark to its cell's points (query seeds).
-    KNN_TRY_CUDA(cudaMemsetAsync(far, 0, cells * 8ull, s));
-    tc_cell_far_kernel<<<ceil_div(n, 256), 256, 0, s>>>(src, stride, dims, k0, n, T.land.as<float>(), ps, far);
-    KNN_LAUNCHED();
-    {
-        std::vector<unsigned long long> hfar(cells);
-        KNN_TRY_CUDA(cudaMemcpyAsync(hfar.data(), far, cells * 8ull, cudaMemcpyDeviceToHost, s));
+
+        // Points by cell (stable), each cell's rows filling whole tiles.
+        bool alt = false;
+        KNN_TRY(radix_sort_pairs(k0, v0, k1, v1, n, static_cast<int>(log2_ceil(cells + 1)), st, s, &alt));
+        const uint32_t* keys = alt ? k1 : k0;
+        const uint32_t* vals = alt ? v1 : v0;
+        std::vector<uint32_t> hkeys(n);
+        KNN_TRY_CUDA(cudaMemcpyAsync(hkeys.data(), keys, n * 4ull, cudaMemcpyDeviceToHost, s));
         KNN_TRY_CUDA(cudaStreamSynchronize(s));
-        std::vector<float> cf(cells);
+        cell_start.assign(cells + 1, 0);
+        cell_tile.assign(cells + 1, 0);
+        for (uint32_t i = 0; i < n; ++i) cell_start[hkeys[i] + 1]++;
         for (uint32_t c = 0; c < cells; ++c) {
-            const uint32_t bits = static_cast<uint32_t>(hfar[c] >> 32);
-            std::memcpy(&cf[c], &bits, 4);
+            cell_tile[c + 1] = cell_tile[c] + ceil_div(cell_start[c + 1], kTileN);
+            cell_start[c + 1] += cell_start[c];
         }
-        KNN_TRY(T.cell_far.alloc(cells * 4ull));
-        KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_far.ptr, cf.data(), cells * 4ull, cudaMemcpyHostToDevice, s));
-        KNN_TRY_CUDA(cudaStreamSynchronize(s));
-    }
+        const uint32_t prows = cell_tile[cells] * kTileN;
+        KNN_TRY(T.cell_start.alloc((cells + 1) * 4ull));
+        KNN_TRY(T.cell_tile.alloc((cells + 1) * 4ull));
+        KNN_TRY(rowmap.alloc(prows * 4ull));
+        KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_start.ptr, cell_start.data(), (cells + 1) * 4ull, cudaMemcpyHostToDevice, s));
+        KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_tile.ptr, cell_tile.data(), (cells + 1) * 4ull, cudaMemcpyHostToDevice, s));
+        KNN_TRY_CUDA(cudaMemsetAsync(rowmap.ptr, 0xFF, prows * 4ull, s));
+        tc_place_kernel<<<ceil_div(n, 256), 256, 0, s>>>(keys, vals, n, T.cell_start.as<uint32_t>(),
+                                                         T.cell_tile.as<uint32_t>(), rowmap.as<uint32_t>());
+        KNN_LAUNCHED();
 
-    // Points by cell (stable), each cell's rows filling whole tiles.
-    bool alt = false;
-    KNN_TRY(radix_sort_pairs(k0, v0, k1, v1, n, static_cast<int>(log2_ceil(cells + 1)), st, s, &alt));
-    const uint32_t* keys = alt ? k1 : k0;
-    const uint32_t* vals = alt ? v1 : v0;
-    std::vector<uint32_t> hkeys(n);
-    KNN_TRY_CUDA(cudaMemcpyAsync(hkeys.data(), keys, n * 4ull, cudaMemcpyDeviceToHost, s));
-    KNN_TRY_CUDA(cudaStreamSynchronize(s));
-    std::vector<uint32_t> cell_start(cells + 1, 0), cell_tile(cells + 1, 0);
-    for (uint32_t i = 0; i < n; ++i) cell_start[hkeys[i] + 1]++;
-    for (uint32_t c = 0; c < cells; ++c) {
-        cell_tile[c + 1] = cell_tile[c] + ceil_div(cell_start[c + 1], kTileN);
-        cell_start[c + 1] += cell_start[c];
+
     }
     const uint32_t ptiles = cell_tile[cells];
     const uint32_t prows = ptiles * kTileN;
     const uint32_t ctiles = ceil_div(cells, kTileN);
+    T.cells = cells;
     T.ptiles = ptiles;
     T.ctiles = ctiles;
-    DevBuf rowmap;
-    KNN_TRY(T.cell_start.alloc((cells + 1) * 4ull));
-    KNN_TRY(T.cell_tile.alloc((cells + 1) * 4ull));
-    KNN_TRY(rowmap.alloc(prows * 4ull));
-    KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_start.ptr, cell_start.data(), (cells + 1) * 4ull, cudaMemcpyHostToDevice, s));
-    KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_tile.ptr, cell_tile.data(), (cells + 1) * 4ull, cudaMemcpyHostToDevice, s));
-    KNN_TRY_CUDA(cudaMemsetAsync(rowmap.ptr, 0xFF, prows * 4ull, s));
-    tc_place_kernel<<<ceil_div(n, 256), 256, 0, s>>>(keys, vals, n, T.cell_start.as<uint32_t>(),
-                                                     T.cell_tile.as<uint32_t>(), rowmap.as<uint32_t>());
-    KNN_LAUNCHED();
 
     // Point operand image, norms, FP32 copy, ids, per-tile norm bounds.
     KNN_TRY(T.img.alloc(static_cast<size_t>(ptiles) * b_bytes(H)));
@@ -1470,13 +1851,21 @@ int tc_prepare(knn_index* ix, cudaStream_t s) {
                                                              T.pmax.as<float>());
     KNN_LAUNCHED();
 
-    // Cell centres and radii (scaled), their operand image and row data.
+    // Cell centres and radii (scaled), their operand image and row data; tree cells' boxes.
     DevBuf cb;
-    KNN_TRY(cb.alloc(carve_bytes({static_cast<size_t>(cells) * ps * 4, cells * 4ull, ctiles * kTileN * 4ull})));
-    Carver cc(cb.ptr);
-    float* centre = cc.take<float>(static_cast<size_t>(cells) * ps);
-    float* radius = cc.take<float>(cells);
-    float* cnorm = cc.take<float>(static_cast<size_t>(ctiles) * kTileN);
+    KNN_TRY(cb.alloc(ctiles * kTileN * 4ull));
+    KNN_TRY(T.ccentre.alloc(static_cast<size_t>(cells) * ps * 4));
+    KNN_TRY(T.cradius.alloc(cells * 4ull));
+    float* centre = T.ccentre.as<float>();
+    float* radius = T.cradius.as<float>();
+    float* cnorm = cb.as<float>();
+    if (T.tree) {
+        T.bd = dims <= 16 ? 16u : 32u;
+        KNN_TRY(T.box.alloc(static_cast<size_t>(cells) * 2 * T.bd * 4));
+        tc_box_kernel<<<ceil_div(cells * 32, 128), 128, 0, s>>>(T.pts.as<float>(), ps, dims, T.scale, T.norm.as<float>(),
+                                                                T.cell_tile.as<uint32_t>(), cells, T.bd, T.box.as<float>());
+        KNN_LAUNCHED();
+    }
     tc_cell_ball_kernel<<<ceil_div(cells * 32, 128), 128, 0, s>>>(T.pts.as<float>(), ps, dims, T.scale, T.norm.as<float>(),
                                                                   T.cell_tile.as<uint32_t>(), cells, rel_margin(dims),
                                                                   centre, radius);
@@ -1499,7 +1888,9 @@ int tc_prepare(knn_index* ix, cudaStream_t s) {
     if (bad) return fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: a point's norm is not finite");
     T.usable = true;
     ix->device_bytes += T.img.bytes + T.norm.bytes + T.pts.bytes + T.ids.bytes + T.pmax.bytes + T.cimg.bytes +
-                        T.cdata.bytes + T.cmax.bytes + T.land.bytes + T.cell_tile.bytes + T.cell_start.bytes;
+                        T.cdata.bytes + T.cmax.bytes + T.land.bytes + T.cell_tile.bytes + T.cell_start.bytes +
+                        T.cell_far.bytes + T.node_dim.bytes + T.node_val.bytes + T.node_leaf.bytes + T.ccentre.bytes +
+                        T.cradius.bytes + T.box.bytes;
     return KNN_OK;
 }
 
@@ -1554,8 +1945,11 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     KNN_TRY_CUDA(cudaMemsetAsync(small, 0, 64 * sizeof(uint32_t), s));
 
     // Queries by cell (rows past the live count sort last), with a seed bound from their cell.
-    KNN_TRY(launch_assign(ix->dp, a.queries, ix->dims, ix->dims, nq, a.order, a.count_dev, T.land.as<float>(), T.ps,
-                          T.cells, k0, v0, s, T.cell_far.as<float>(), T.cell_start.as<uint32_t>(), a.k, seed));
+    if (T.tree)
+        KNN_TRY(launch_descend(ix->dp, a.queries, ix->dims, nq, a.order, a.count_dev, T, a.k, k0, v0, seed, s));
+    else
+        KNN_TRY(launch_assign(ix->dp, a.queries, ix->dims, ix->dims, nq, a.order, a.count_dev, T.land.as<float>(), T.ps,
+                              T.cells, k0, v0, s, T.cell_far.as<float>(), T.cell_start.as<uint32_t>(), a.k, seed));
     bool alt = false;
     KNN_TRY(radix_sort_pairs(k0, v0, k1, v1, nq, static_cast<int>(log2_ceil(T.cells + 1)), st, s, &alt));
     const uint32_t* cell_sorted = alt ? k1 : k0;
@@ -1580,6 +1974,10 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     p.cmax = T.cmax.as<float>();
     p.cell_tile = T.cell_tile.as<uint32_t>();
     p.qhome = qhome;
+    p.box = T.tree ? T.box.as<float>() : nullptr;
+    p.queries = a.queries;
+    p.dims = ix->dims;
+    p.scale = T.scale;
     p.cells = T.cells;
     p.ctiles = T.ctiles;
     p.nq = nq;
@@ -1602,8 +2000,11 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     p.error = reinterpret_cast<int*>(small + 1);
     const size_t smem = filter_launch_smem(H, a.k);
     const uint32_t acc = accumulators(H, a.k);
-    auto kern = H == 1 ? (acc == 1 ? tc_filter_kernel<1, 1> : tc_filter_kernel<1, 2>)
-                       : (acc == 1 ? tc_filter_kernel<2, 1> : tc_filter_kernel<2, 2>);
+    void (*kern)(const TcParams) = nullptr;
+    if (T.tree && T.bd == 16) kern = acc == 1 ? tc_filter_kernel<1, 1, 16> : tc_filter_kernel<1, 2, 16>;
+    else if (T.tree) kern = acc == 1 ? tc_filter_kernel<1, 1, 32> : tc_filter_kernel<1, 2, 32>;
+    else if (H == 1) kern = acc == 1 ? tc_filter_kernel<1, 1, 0> : tc_filter_kernel<1, 2, 0>;
+    else kern = acc == 1 ? tc_filter_kernel<2, 1, 0> : tc_filter_kernel<2, 2, 0>;
     KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));
     kern<<<qtiles, kThreads, smem, s>>>(p);

@@ -183,6 +183,11 @@ struct knn_index {
     //          norms and radii (scaled), and an upper bound on the centres' norms
     struct TensorCoreState {
         knn::DevBuf img, norm, pts, ids, pmax, land, cell_start, cell_tile, cell_far, cimg, cdata, cmax, ws;
+        // Tree layout (low dims): per tree node its split dimension, value and leaf cell (-1 for
+        // splits); per cell its centre and radius (scaled) and box [2][bd] (scaled minima, maxima).
+        knn::DevBuf node_dim, node_val, node_leaf, ccentre, cradius, box;
+        bool tree = false;
+        uint32_t bd = 0;
         uint32_t cells = 0, ptiles = 0, ctiles = 0, ps = 0;
         bool f16 = true;
         float scale = 1.0f;   // power of two applied before rounding to FP16
