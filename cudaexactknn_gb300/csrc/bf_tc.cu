@@ -666,6 +666,7 @@ __device__ __forceinline__ void warp_bitonic(uint64_t* buf, uint32_t n, uint32_t
 template <int PS>
 __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const RescoreArgs a) {
     __shared__ uint64_t sbuf[kRescoreWarps][kRescoreBuf];
+    __shared__ float4 sq[kRescoreWarps][PS / 4];
     const uint32_t lane = threadIdx.x % 32, w = threadIdx.x / 32;
     const uint32_t r = blockIdx.x * kRescoreWarps + w;  // row of the sorted batch
     if (r >= (a.live_count ? *a.live_count : a.nq)) return;  // warp-uniform
@@ -683,9 +684,11 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
         }
         return;
     }
-    float qv[PS];
-#pragma unroll
-    for (int d = 0; d < PS; ++d) qv[d] = static_cast<uint32_t>(d) < a.dims ? a.queries[static_cast<size_t>(qi) * a.dims + d] : 0.0f;
+    // The query, zero padded, in shared memory: every lane reads it (broadcast).
+    float* sqf = reinterpret_cast<float*>(sq[w]);
+    for (uint32_t d = lane; d < static_cast<uint32_t>(PS); d += 32)
+        sqf[d] = d < a.dims ? a.queries[static_cast<size_t>(qi) * a.dims + d] : 0.0f;
+    __syncwarp();
     const float r2 = a.radii ? fminf(a.radii[qi], a.max_d2) : a.max_d2;
     const uint64_t limit = make_key(r2, -1);  // the key an unfilled slot holds
     const Bounds& b = a.b;
@@ -725,7 +728,7 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
             const float4* ra = reinterpret_cast<const float4*>(a.pts + static_cast<size_t>(na ? pa : pb) * PS);
             const float4* rb = reinterpret_cast<const float4*>(a.pts + static_cast<size_t>(nb ? pb : pa) * PS);
             float da, db;
-            dist2_vec4_pair<PS>(qv, ra, rb, &da, &db);
+            dist2_vec4_pair_sq<PS>(sq[w], ra, rb, &da, &db);
             if (na) ka = make_key(da, static_cast<int32_t>(a.ids[pa]));
             if (nb) kb = make_key(db, static_cast<int32_t>(a.ids[pb]));
             scored += (na ? 1u : 0u) + (nb ? 1u : 0u);
@@ -954,17 +957,38 @@ __global__ void __launch_bounds__(128) tc_assign_kernel(const float* __restrict_
         }
         __syncthreads();
         const uint32_t jn = min(kChunk, cells - c0);
-        for (uint32_t j = 0; j < jn; ++j) {
+        // Two landmarks at a time, four partial sums each (the assignment may pick any landmark,
+        // and the seed's error margin holds for any summation order).
+        auto consider = [&](float acc, uint32_t j) {
+            if (acc < best) {
+                best = acc;
+                bi = c0 + j;
+            }
+        };
+        uint32_t j = 0;
+        for (; j + 1 < jn; j += 2) {
+            float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f, b0 = 0.0f, b1 = 0.0f, b2 = 0.0f, b3 = 0.0f;
+#pragma unroll
+            for (int d = 0; d < DP; ++d) {
+                const float t = __fsub_rn(q[d], sl[j * DP + d]), u = __fsub_rn(q[d], sl[(j + 1) * DP + d]);
+                switch (d & 3) {
+                    case 0: a0 = __fmaf_rn(t, t, a0); b0 = __fmaf_rn(u, u, b0); break;
+                    case 1: a1 = __fmaf_rn(t, t, a1); b1 = __fmaf_rn(u, u, b1); break;
+                    case 2: a2 = __fmaf_rn(t, t, a2); b2 = __fmaf_rn(u, u, b2); break;
+                    default: a3 = __fmaf_rn(t, t, a3); b3 = __fmaf_rn(u, u, b3); break;
+                }
+            }
+            consider((a0 + a1) + (a2 + a3), j);
+            consider((b0 + b1) + (b2 + b3), j + 1);
+        }
+        if (j < jn) {
             float acc = 0.0f;
 #pragma unroll
             for (int d = 0; d < DP; ++d) {
                 const float t = __fsub_rn(q[d], sl[j * DP + d]);
                 acc = __fmaf_rn(t, t, acc);
             }
-            if (acc < best) {
-                best = acc;
-                bi = c0 + j;
-            }
+            consider(acc, j);
         }
     }
     if (r < rows) {
