@@ -4,16 +4,19 @@
 // The reference computes every pair's distance with SIMT FP32 (src/BruteForceGpu.cuh:9-31) or
 // walks a tree per query (src/KdTreeGpu.cuh:392-410, src/BallTreeGpu.cuh:630-648).  Here:
 //
-// Layout, once per index.  Landmarks (every (n/L)-th point, L about n/1024; cells much wider
-// than the median cell get a second landmark at their farthest point, twice) split the points
-// into Voronoi cells.  The points are laid out cell by cell in tiles of 256 rows, each cell's last
-// tile padded.  Every cell gets a centre (the mean of its points) and a radius bounding the
+// Layout, once per index.  Up to 32 dims, the cells are the leaves of a tile-aligned partition
+// tree (each node sends the first half of its tiles, by its widest dimension, to the left child),
+// so every cell is a compact run of whole tiles with a tight axis-aligned box.  Beyond 32 dims,
+// landmarks (every (n/L)-th point, L about n/1024; cells much wider than the median cell get a
+// second landmark at their farthest point, twice) split the points into Voronoi cells.  The points
+// are laid out cell by cell in tiles of 256 rows, each cell's last tile padded (tree cells have
+// only the last tile of all partial).  Every cell gets a centre (the mean of its points) and a radius bounding the
 // exact distance from the centre to each of its points.  The operand images hold every row, and
 // every cell centre, scaled by s = 2^e (e >= 0, largest |coordinate| * s in [2^13, 2^14)) and
 // rounded to FP16; data whose largest |coordinate| exceeds 2^14 uses BF16 with s = 1.
 //
-// Per query batch.  Each query goes to its nearest landmark's cell and the batch is sorted by
-// cell.  A run of 128 sorted queries (a query tile) has a home range: the cells of its queries,
+// Per query batch.  Each query goes to its cell (the leaf it descends to, or its nearest
+// landmark's cell) and the batch is sorted by cell.  A run of 128 sorted queries (a query tile) has a home range: the cells of its queries,
 // widened by whole cells to at least max(2k, 512) points.  One CTA per query tile, over a
 // sequence of 256-row tiles:
 //   phase 1   the home tiles: each query's running k-th upper bound T;

@@ -77,7 +77,9 @@ typedef enum knn_structure {
 #define KNN_QF_AUTOTUNE 2u       /* engine picks block size, tracking, storage and leaf size */
 #define KNN_QF_LEARNED_RADIUS 4u /* seed each query's radius from the trained model; queries
                                     with fewer than k hits are re-run unbounded */
-#define KNN_QF_BF16_FILTER 8u    /* brute force, dims >= 16: BF16 tensor-core filter + FP32 rescore */
+#define KNN_QF_BF16_FILTER 8u    /* any index, dims >= 16: 16-bit (FP16, or BF16 for values beyond
+                                    FP16's range) tcgen05 filter with rigorous bounds + exact FP32
+                                    rescore; the same answer as the plain search */
 #define KNN_QF_KEEP_ORDER 16u    /* do not reorder queries for locality */
 #define KNN_QF_TIMING 32u        /* record CUDA events around the query and its search kernel */
 
@@ -97,7 +99,8 @@ typedef struct knn_query_opts {
                                leaf (0 = the tree's own leaves) */
     uint32_t traversal;     /* trees: 0 = one depth-first search per thread (the reference's
                                scheme), 1 = warp-coherent search (a warp's queries walk together) */
-    uint32_t reserved;      /* KNN_QF_BF16_FILTER: candidates kept per query (0 = 4096); for
+    uint32_t reserved;      /* KNN_QF_BF16_FILTER: candidates kept per query (0 = the engine's
+                               default, min(4096, max(1024, 16 k))); for
                                knn_tuned_plan, the number of candidate plans timed */
 } knn_query_opts;
 
@@ -191,7 +194,8 @@ typedef struct knn_batch_item {
 } knn_batch_item;
 /* Plans a batch: items grouped by (tree, dims, k) class, one persistent kernel per class over all
  * its sets, the classes captured as parallel branches of one CUDA graph.  flags: KNN_QF_AUTOTUNE
- * tunes each class on its largest set (runs queries, synchronously); KNN_QF_KEEP_ORDER skips the
+ * tunes each class on its largest set (runs queries, synchronously) and sends a class of dims >= 16
+ * through the tensor-core filter when that times faster; KNN_QF_KEEP_ORDER skips the
  * locality sort.  The items' pointers are baked into the graph: refill the buffers, not the items. */
 KNN_API int knn_batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, void* stream,
                              knn_batch** out);
