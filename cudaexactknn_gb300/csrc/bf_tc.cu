@@ -626,7 +626,7 @@ struct RescoreArgs {
     const float* radii;
     const uint32_t* order;       // row -> query index
     const uint32_t* live_count;  // rows in use (device), or null for nq
-    const uint32_t* cand;
+    uint32_t* cand;           // per row: candidate positions (compacted in place by the rescoring)
     const float* cand_v;
     const uint32_t* cand_count;
     const float* qnorm;       // per row: scaled norm of the query
@@ -639,12 +639,31 @@ struct RescoreArgs {
     float* retry_r2;          // per query index: the radius its plain search may use
     float inv_s2;             // 1 / s^2
     DevCounters* counters;
+    uint32_t buf;             // keys buffered per warp (rescore_buf(k))
+    uint32_t warp_bytes;      // shared memory per warp
 };
 
-constexpr uint32_t kRescoreWarps = 4;
-constexpr uint32_t kRescoreBuf = 1024;  // keys buffered per warp before a sort-and-trim
+constexpr uint32_t kRescoreWarps = 4;  // most warps per block (one row each)
 
-// Sorts buf[0, n) ascending (n a power of two, <= kRescoreBuf) with the lanes of one warp.
+// Staging of candidate rows in shared memory: each warp copies the rows of 32 candidates at a time
+// with coalesced 16-byte copies (one row of PS floats = kV lanes' worth), into slots of an odd
+// number of 16-byte units so that lane l reading slot l with 16-byte loads hits distinct banks.
+template <int PS>
+struct RescoreShape {
+    static constexpr uint32_t kV = PS / 4;                       // 16-byte units per row
+    static constexpr uint32_t kSlot = (kV % 2) ? kV : kV + 1;    // 16-byte units per staged row
+    static constexpr uint32_t kRowsPerCopy = 32 / kV;            // rows one warp-wide copy moves
+    static constexpr uint32_t kStageBytes = 32 * kSlot * 16;     // 32 candidates
+};
+
+// Keys buffered per warp before a sort-and-trim: room for k kept keys plus one step of 32.
+inline uint32_t rescore_buf(uint32_t k) {
+    uint32_t b = 64;
+    while (b < k + 32) b <<= 1;
+    return b;
+}
+
+// Sorts buf[0, n) ascending (n a power of two) with the lanes of one warp.
 __device__ __forceinline__ void warp_bitonic(uint64_t* buf, uint32_t n, uint32_t lane) {
     for (uint32_t size = 2; size <= n; size <<= 1) {
         for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
@@ -663,17 +682,42 @@ __device__ __forceinline__ void warp_bitonic(uint64_t* buf, uint32_t n, uint32_t
     }
 }
 
-// One warp per row.  Lanes take candidates in turn; each kept candidate's exact distance is
-// computed by one lane (the reference's sequential sum over the dims), its key appended to the
-// warp's buffer; a full buffer is sorted and trimmed to the k smallest keys.
+// The reference's sequential FP32 squared-difference sum of a query and a point row, both in shared
+// memory (zero padded to PS: the padding adds fma(0, 0, acc) = acc).
+template <int PS>
+__device__ __forceinline__ float dist2_smem(const float4* __restrict__ q4, const float4* __restrict__ p4) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int v = 0; v < PS / 4; ++v) {
+        const float4 q = q4[v], x = p4[v];
+        float t = __fsub_rn(q.x, x.x);
+        acc = __fmaf_rn(t, t, acc);
+        t = __fsub_rn(q.y, x.y);
+        acc = __fmaf_rn(t, t, acc);
+        t = __fsub_rn(q.z, x.z);
+        acc = __fmaf_rn(t, t, acc);
+        t = __fsub_rn(q.w, x.w);
+        acc = __fmaf_rn(t, t, acc);
+    }
+    return acc;
+}
+
+// One warp per row.  Phase 1 tests every candidate's GEMM lower bound and compacts the ones that
+// must be rescored.  Phase 2 takes them 32 per step, one per lane: the warp copies their rows into
+// one of two shared-memory stages (the copies of step j + 1 are in flight while step j is scored),
+// each lane sums its own row in dimension order and the keys go to the warp's buffer; a full
+// buffer is sorted and trimmed to the k smallest keys.
 template <int PS>
 __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const RescoreArgs a) {
-    __shared__ uint64_t sbuf[kRescoreWarps][kRescoreBuf];
-    __shared__ float4 sq[kRescoreWarps][PS / 4];
+    using Sh = RescoreShape<PS>;
+    extern __shared__ __align__(16) uint8_t rs_smem[];
     const uint32_t lane = threadIdx.x % 32, w = threadIdx.x / 32;
-    const uint32_t r = blockIdx.x * kRescoreWarps + w;  // row of the sorted batch
+    const uint32_t r = blockIdx.x * (blockDim.x / 32) + w;  // row of the sorted batch
     if (r >= (a.live_count ? *a.live_count : a.nq)) return;  // warp-uniform
-    uint64_t* buf = sbuf[w];
+    uint8_t* mine = rs_smem + static_cast<size_t>(w) * a.warp_bytes;
+    float4* stage = reinterpret_cast<float4*>(mine);                                   // [2][32][kSlot]
+    float4* sq = reinterpret_cast<float4*>(mine + 2 * Sh::kStageBytes);               // [PS / 4]
+    uint64_t* buf = reinterpret_cast<uint64_t*>(mine + 2 * Sh::kStageBytes + PS * 4);  // [a.buf]
     const uint32_t qi = a.order[r];
     const uint32_t cnt = a.cand_count[r];
     if (cnt > a.cap) {
@@ -688,10 +732,9 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
         return;
     }
     // The query, zero padded, in shared memory: every lane reads it (broadcast).
-    float* sqf = reinterpret_cast<float*>(sq[w]);
+    float* sqf = reinterpret_cast<float*>(sq);
     for (uint32_t d = lane; d < static_cast<uint32_t>(PS); d += 32)
         sqf[d] = d < a.dims ? a.queries[static_cast<size_t>(qi) * a.dims + d] : 0.0f;
-    __syncwarp();
     const float r2 = a.radii ? fminf(a.radii[qi], a.max_d2) : a.max_d2;
     const uint64_t limit = make_key(r2, -1);  // the key an unfilled slot holds
     const Bounds& b = a.b;
@@ -701,66 +744,111 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
     const float one_m_g = __fsub_rd(1.0f, b.g);
     const float c1q = __fmul_ru(b.c1, qup);
     const float tfin = a.final_t[r];
-    const uint32_t* c = a.cand + static_cast<size_t>(r) * a.cap;
+    uint32_t* c = a.cand + static_cast<size_t>(r) * a.cap;
     const float* cv = a.cand_v + static_cast<size_t>(r) * a.cap;
-    uint32_t m = 0, scored = 0;
-    // Whether candidate i must be rescored: its GEMM lower bound does not exceed T'.
-    auto needed = [&](uint32_t i, uint32_t* pos) {
-        if (i >= cnt) return false;
-        *pos = c[i];
-        const float pm = __ldg(a.pmax + *pos / kTileN);
-        const float E = __fadd_ru(__fmaf_ru(c1q, pm, __fmul_ru(b.c3, __fadd_ru(qup, pm))), b.c4);
-        // Lower bound of s^2 times the pair's float distance.
-        const float lo = __fsub_rd(__fmaf_rd(-2.0f, cv[i], __fmul_rd(one_m_gn, __fadd_rd(nq, __ldg(a.pnorm + *pos)))),
-                                   __fmul_ru(2.0f, E));
-        return !(__fmul_rd(__fsub_rd(lo, b.c4), one_m_g) > tfin);
-    };
-    auto append = [&](uint64_t key) {
-        const bool take = key < limit;
-        const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, take);
-        if (take) buf[m + __popc(ballot & ((1u << lane) - 1u))] = key;
-        m += __popc(ballot);
-        __syncwarp();
-    };
-    // Two candidates per lane per step, their distance chains interleaved.
-    for (uint32_t i0 = 0; i0 < cnt; i0 += 64) {
-        uint32_t pa = 0, pb = 0;
-        const bool na = needed(i0 + lane, &pa), nb = needed(i0 + 32 + lane, &pb);
-        uint64_t ka = ~0ull, kb = ~0ull;
-        if (na || nb) {
-            const float4* ra = reinterpret_cast<const float4*>(a.pts + static_cast<size_t>(na ? pa : pb) * PS);
-            const float4* rb = reinterpret_cast<const float4*>(a.pts + static_cast<size_t>(nb ? pb : pa) * PS);
-            float da, db;
-            dist2_vec4_pair_sq<PS>(sq[w], ra, rb, &da, &db);
-            if (na) ka = make_key(da, static_cast<int32_t>(a.ids[pa]));
-            if (nb) kb = make_key(db, static_cast<int32_t>(a.ids[pb]));
-            scored += (na ? 1u : 0u) + (nb ? 1u : 0u);
+    // Phase 1: keep the candidates whose GEMM lower bound (s^2 times a lower bound of the pair's
+    // float distance) does not exceed T', compacted in place at the front of the list.  Four
+    // groups of 32 per pass, their loads independent.
+    uint32_t kept = 0;
+    for (uint32_t i0 = 0; i0 < cnt; i0 += 128) {
+        uint32_t pos[4];
+        float v[4], pm[4], pn[4];
+#pragma unroll
+        for (uint32_t u = 0; u < 4; ++u) {
+            const uint32_t i = i0 + 32 * u + lane;
+            pos[u] = i < cnt ? c[i] : 0u;
+            v[u] = i < cnt ? cv[i] : 0.0f;
         }
-        if (m + 64 > kRescoreBuf) {
+#pragma unroll
+        for (uint32_t u = 0; u < 4; ++u) {
+            pm[u] = __ldg(a.pmax + pos[u] / kTileN);
+            pn[u] = __ldg(a.pnorm + pos[u]);
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < 4; ++u) {
+            const float E = __fadd_ru(__fmaf_ru(c1q, pm[u], __fmul_ru(b.c3, __fadd_ru(qup, pm[u]))), b.c4);
+            const float lo = __fsub_rd(__fmaf_rd(-2.0f, v[u], __fmul_rd(one_m_gn, __fadd_rd(nq, pn[u]))),
+                                       __fmul_ru(2.0f, E));
+            const bool keep = i0 + 32 * u + lane < cnt && !(__fmul_rd(__fsub_rd(lo, b.c4), one_m_g) > tfin);
+            // The ballot orders every lane's loads of this pass before any lane's store below.
+            const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, keep);
+            if (keep) c[kept + __popc(ballot & ((1u << lane) - 1u))] = pos[u];
+            kept += __popc(ballot);
+        }
+    }
+    __syncwarp();  // the compacted list and the query are visible to every lane
+    // Phase 2: the kept rows, 32 per step, staged in shared memory and summed one per lane.
+    auto stage_rows = [&](uint32_t st, uint32_t mask, uint32_t pos) {
+        float4* dst = stage + st * 32 * Sh::kSlot;
+        const uint32_t sub = lane / Sh::kV, v = lane % Sh::kV;
+#pragma unroll 4
+        for (uint32_t g = 0; g < 32; g += Sh::kRowsPerCopy) {
+            uint32_t grp;
+            if constexpr (Sh::kRowsPerCopy == 32) grp = mask;
+            else grp = (mask >> g) & ((1u << Sh::kRowsPerCopy) - 1u);
+            if (grp == 0) continue;  // warp-uniform
+            const uint32_t slot = g + sub;
+            const uint32_t src = __shfl_sync(0xFFFFFFFFu, pos, slot);
+            if ((mask >> slot) & 1u) cp_async16(dst + slot * Sh::kSlot + v, a.pts + static_cast<size_t>(src) * PS + 4 * v);
+        }
+        cp_async_commit();
+    };
+    const uint32_t steps = (kept + 31) / 32;
+    uint32_t m = 0;  // keys in the buffer
+    bool need_c = lane < kept;
+    uint32_t pos_c = need_c ? c[lane] : 0u;
+    uint32_t id_c = need_c ? a.ids[pos_c] : 0u;
+    if (steps) stage_rows(0, __ballot_sync(0xFFFFFFFFu, need_c), pos_c);
+    for (uint32_t j = 0; j < steps; ++j) {
+        uint32_t pos_n = 0, id_n = 0;
+        bool need_n = false;
+        if (j + 1 < steps) {
+            need_n = 32 * (j + 1) + lane < kept;
+            if (need_n) {
+                pos_n = c[32 * (j + 1) + lane];
+                id_n = a.ids[pos_n];
+            }
+            stage_rows((j + 1) & 1, __ballot_sync(0xFFFFFFFFu, need_n), pos_n);
+        } else {
+            cp_async_commit();  // an empty group: the wait below always leaves the newest one
+        }
+        cp_async_wait<1>();
+        __syncwarp();  // every lane's copies of step j have landed
+        uint64_t key = ~0ull;
+        if (need_c) key = make_key(dist2_smem<PS>(sq, stage + (j & 1) * 32 * Sh::kSlot + lane * Sh::kSlot),
+                                   static_cast<int32_t>(id_c));
+        if (m + 32 > a.buf) {
             // Sort and keep the k smallest (the rest cannot be in the answer).
             uint32_t n2 = 1;
             while (n2 < m) n2 <<= 1;
-            for (uint32_t j = m + lane; j < n2; j += 32) buf[j] = ~0ull;
+            for (uint32_t t = m + lane; t < n2; t += 32) buf[t] = ~0ull;
             __syncwarp();
             warp_bitonic(buf, n2, lane);
             m = min(m, a.k);
         }
-        append(ka);
-        append(kb);
+        const bool take = key < limit;
+        const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, take);
+        if (take) buf[m + __popc(ballot & ((1u << lane) - 1u))] = key;
+        m += __popc(ballot);
+        __syncwarp();  // stage j & 1 is read before step j + 2's copies overwrite it
+        pos_c = pos_n;
+        id_c = id_n;
+        need_c = need_n;
     }
+    cp_async_wait<0>();
     uint32_t n2 = 1;
     while (n2 < m) n2 <<= 1;
-    for (uint32_t j = m + lane; j < n2; j += 32) buf[j] = ~0ull;
+    for (uint32_t t = m + lane; t < n2; t += 32) buf[t] = ~0ull;
     __syncwarp();
     if (m > 1) warp_bitonic(buf, n2, lane);
-    for (uint32_t j = lane; j < a.k; j += 32) {
-        const uint64_t key = j < m ? buf[j] : limit;
-        a.out_idx[static_cast<size_t>(qi) * a.k + j] = j < m ? key_index(key) : -1;
-        a.out_dist[static_cast<size_t>(qi) * a.k + j] = j < m ? key_dist(key) : r2;
+    for (uint32_t t = lane; t < a.k; t += 32) {
+        const uint64_t key = t < m ? buf[t] : limit;
+        a.out_idx[static_cast<size_t>(qi) * a.k + t] = t < m ? key_index(key) : -1;
+        a.out_dist[static_cast<size_t>(qi) * a.k + t] = t < m ? key_dist(key) : r2;
     }
-    if (a.counters) {
-        for (int o = 16; o; o >>= 1) scored += __shfl_xor_sync(0xFFFFFFFFu, scored, o);
-        if (lane == 0) atomicAdd(&a.counters->nodes, static_cast<unsigned long long>(scored));
+    if (a.counters && lane == 0) {
+        atomicAdd(&a.counters->nodes, static_cast<unsigned long long>(kept));
+        atomicAdd(&a.counters->points, static_cast<unsigned long long>(cnt));
     }
 }
 
@@ -1459,6 +1547,149 @@ Bounds make_bounds(uint32_t dims, bool f16, float scale) {
     return b;
 }
 
+// Cell of each query at query time (landmark layout): the nearest landmark by the 16-bit GEMM,
+// one CTA per 128 rows.  Thread 0 streams the rows' operand tile and every landmark tile (with its
+// 256 scaled norms) through a two-stage ring and issues the MMAs; all four warps read the
+// accumulator (thread = row) and keep the column of least n_l - 2G.  Any cell is a correct choice
+// (every later bound holds for any assignment); the nearest landmark's cell is the one whose
+// points lie around the query.  The seed is then (|x - l| + far_l)^2 over that cell when it holds
+// >= k points, from the row's float distance to the landmark (rounded up, margins g for the float
+// distances and 2^-120 for subnormal ones).
+// Rows past the live count get key `cells`.  Every wait is bounded; a timeout sets *error and the
+// rows keep the best cell seen so far, with no seed.
+template <uint32_t H>
+__global__ void __launch_bounds__(128, 1) tc_assign_mma_kernel(
+    const uint8_t* __restrict__ qimg, const uint8_t* __restrict__ limg, const float* __restrict__ lnorm,
+    uint32_t ctiles, uint32_t cells, uint32_t idesc, uint32_t rows, const uint32_t* __restrict__ order,
+    const uint32_t* __restrict__ live_count, const float* __restrict__ queries, uint32_t dims,
+    const float* __restrict__ land, uint32_t ps, const float* __restrict__ cell_far,
+    const uint32_t* __restrict__ cell_start, uint32_t k, uint32_t* __restrict__ keys,
+    uint32_t* __restrict__ vals, float* __restrict__ seed, int* __restrict__ error) {
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = smem_addr(smem_raw);
+    uint8_t* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    uint8_t* sA = smem;
+    uint8_t* sB = sA + a_bytes(H);                                              // [2] landmark tiles
+    float* sN = reinterpret_cast<float*>(sB + 2 * b_bytes(H));                 // [2][kTileN] norms
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sN + 2 * kTileN);               // [0..1] loads, [2] MMA
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 3);
+    volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint32_t tile = blockIdx.x;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        mbar_init(bar + 1, 1);
+        mbar_init(bar + 2, 1);
+        *abort = 0;
+        mbar_fence_init();
+    }
+    if (warp == 0) tmem_alloc(tmem_slot, kTileN);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    uint32_t loads_issued = 0, loads_done = 0, commits = 0;  // thread 0's counts
+    auto load_centres = [&](uint32_t t) {  // thread 0
+        const uint32_t st = t & 1;
+        ++loads_issued;
+        mbar_expect_tx(bar + st, b_bytes(H) + kTileN * 4 + (t == 0 ? a_bytes(H) : 0u));
+        if (t == 0) bulk_copy_g2s(sA, qimg + static_cast<size_t>(tile) * a_bytes(H), a_bytes(H), bar);
+        bulk_copy_g2s(sB + st * b_bytes(H), limg + static_cast<size_t>(t) * b_bytes(H), b_bytes(H), bar + st);
+        bulk_copy_g2s(sN + st * kTileN, lnorm + static_cast<size_t>(t) * kTileN, kTileN * 4, bar + st);
+    };
+    if (threadIdx.x == 0) {
+        load_centres(0);
+        if (ctiles > 1) load_centres(1);
+    }
+    float best = INFINITY;
+    uint32_t bi = 0;
+    for (uint32_t t = 0; t < ctiles; ++t) {
+        const uint32_t st = t & 1;
+        if (threadIdx.x == 0) {
+            if (!*abort && mbar_wait(bar + st, (t >> 1) & 1u, abort)) {
+                ++loads_done;
+                tc_fence_after();
+                for (uint32_t h = 0; h < H; ++h)
+                    for (uint32_t kk = 0; kk < 4; ++kk)
+                        mma_f16kind(tmem, desc_sw128(smem_addr(sA) + h * kTileM * 128u + kk * 32u),
+                                    desc_sw128(smem_addr(sB + st * b_bytes(H)) + h * kTileN * 128u + kk * 32u), idesc,
+                                    (h | kk) != 0);
+                mma_commit(bar + 2);
+                ++commits;
+            } else {
+                *abort = 1;
+            }
+        }
+        __syncthreads();
+        const bool failed = *abort || !mbar_wait(bar + 2, t & 1u, abort);
+        if (__syncthreads_or(failed)) {  // every thread leaves the loop at the same tile
+            if (threadIdx.x == 0) *abort = 1;
+            break;
+        }
+        tc_fence_after();
+        const float* nrm = sN + st * kTileN;
+        for (uint32_t c = 0; c < kTileN / 32; ++c) {
+            float v[32];
+            tmem_ld32(tmem + ((warp * 32u) << 16) + c * 32, v);
+#pragma unroll
+            for (uint32_t i = 0; i < 32; ++i) {
+                const float d = __fmaf_rn(-2.0f, v[i], nrm[c * 32 + i]);
+                if (d < best) {
+                    best = d;
+                    bi = t * kTileN + c * 32 + i;
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();  // the accumulator and stage st are free
+        if (threadIdx.x == 0 && t + 2 < ctiles) load_centres(t + 2);
+    }
+    __syncthreads();
+    const bool aborted = *abort != 0;
+    if (aborted && threadIdx.x == 0) {
+        atomicExch(error, 1);
+        // Let the copies and MMAs still in flight land before the block's memory is released.
+        volatile int never = 0;
+        for (uint32_t i = loads_done; i < loads_issued; ++i) mbar_wait(bar + (i & 1), (i >> 1) & 1u, &never);
+        if (commits) mbar_wait(bar + 2, (commits - 1) & 1u, &never);
+    }
+    // Every row gets a valid cell, also after a timeout (any cell is correct).
+    const uint32_t r = tile * kTileM + warp * 32 + lane;
+    if (r < rows) {
+        const bool live = r < (live_count ? *live_count : rows);
+        const uint32_t qi = live ? (order ? order[r] : r) : 0u;
+        const uint32_t c = min(bi, cells - 1);
+        keys[r] = live ? c : cells;
+        vals[r] = qi;
+        if (live && seed) {
+            float t = INFINITY;
+            if (!aborted && cell_start[c + 1] - cell_start[c] >= k) {
+                float acc = 0.0f;
+                for (uint32_t d = 0; d < dims; ++d) {
+                    const float e = __fsub_rn(queries[static_cast<size_t>(qi) * dims + d], land[static_cast<size_t>(c) * ps + d]);
+                    acc = __fmaf_rn(e, e, acc);
+                }
+                if (acc <= FLT_MAX) {
+                    const float g = rel_margin(dims);
+                    const float inv = __frcp_ru(__fsub_rd(1.0f, g));  // >= 1 / (1 - g)
+                    const float a = __fsqrt_ru(__fmul_ru(acc, inv));   // >= exact |x - l|
+                    const float b = __fsqrt_ru(__fmul_ru(cell_far[c], inv));
+                    t = __fadd_ru(__fmul_ru(__fmul_ru(__fadd_ru(a, b), __fadd_ru(a, b)), __fadd_ru(1.0f, g)), 0x1p-120f);
+                }
+            }
+            seed[qi] = t;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, kTileN);
+    }
+}
+
+size_t assign_mma_smem(uint32_t H) { return 1024 + a_bytes(H) + 2 * b_bytes(H) + 2 * kTileN * 4 + 64; }
+
 int launch_assign(uint32_t dp, const float* src, uint32_t stride, uint32_t dims, uint32_t rows, const uint32_t* order,
                   const uint32_t* live_count, const float* land, uint32_t ps, uint32_t cells, uint32_t* keys,
                   uint32_t* vals, cudaStream_t s, const float* cell_far = nullptr, const uint32_t* cell_start = nullptr,
@@ -1826,6 +2057,19 @@ int tc_prepare(knn_index* ix, cudaStream_t s) {
             KNN_TRY_CUDA(cudaMemcpyAsync(T.cell_far.ptr, cf.data(), cells * 4ull, cudaMemcpyHostToDevice, s));
             KNN_TRY_CUDA(cudaStreamSynchronize(s));
         }
+        // The landmarks as a 16-bit operand image with their scaled norms (+inf on padding), for
+        // the query-time assignment GEMM.
+        {
+            const uint32_t ltiles = ceil_div(cells, kTileN);
+            KNN_TRY(T.limg.alloc(static_cast<size_t>(ltiles) * b_bytes(H)));
+            KNN_TRY(T.lnorm.alloc(static_cast<size_t>(ltiles) * kTileN * 4));
+            tc_pack_kernel<<<ceil_div(ltiles * kTileN, 128), 128, 0, s>>>(T.land.as<float>(), ps, dims, nullptr, cells,
+                                                                          nullptr, kTileN, H, T.f16, T.scale,
+                                                                          T.limg.as<uint8_t>(), T.lnorm.as<float>(),
+                                                                          INFINITY, nullptr, 0, nullptr, nullptr,
+                                                                          ltiles * kTileN, nullptr);
+            KNN_LAUNCHED();
+        }
 
 
         // Points by cell (stable), each cell's rows filling whole tiles.
@@ -1916,14 +2160,21 @@ int tc_prepare(knn_index* ix, cudaStream_t s) {
     T.usable = true;
     ix->device_bytes += T.img.bytes + T.norm.bytes + T.pts.bytes + T.ids.bytes + T.pmax.bytes + T.cimg.bytes +
                         T.cdata.bytes + T.cmax.bytes + T.land.bytes + T.cell_tile.bytes + T.cell_start.bytes +
-                        T.cell_far.bytes + T.node_dim.bytes + T.node_val.bytes + T.node_leaf.bytes + T.ccentre.bytes +
+                        T.cell_far.bytes + T.limg.bytes + T.lnorm.bytes + T.node_dim.bytes + T.node_val.bytes + T.node_leaf.bytes + T.ccentre.bytes +
                         T.cradius.bytes + T.box.bytes;
     return KNN_OK;
 }
 
 template <int PS>
-static int rescore(const RescoreArgs& ra, uint32_t count, cudaStream_t s) {
-    tc_rescore_kernel<PS><<<ceil_div(count, kRescoreWarps), 32 * kRescoreWarps, 0, s>>>(ra);
+static int rescore(RescoreArgs ra, uint32_t count, cudaStream_t s) {
+    ra.buf = rescore_buf(ra.k);
+    ra.warp_bytes = 2 * RescoreShape<PS>::kStageBytes + PS * 4 + ra.buf * 8;
+    // Two warps per block at the widest rows (about 36 KB of stages and buffer each), else four.
+    const uint32_t warps = ra.warp_bytes > 24576 ? 2 : kRescoreWarps;
+    const size_t smem = static_cast<size_t>(warps) * ra.warp_bytes;
+    KNN_TRY_CUDA(cudaFuncSetAttribute(tc_rescore_kernel<PS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem)));
+    tc_rescore_kernel<PS><<<ceil_div(count, warps), 32 * warps, smem, s>>>(ra);
     KNN_LAUNCHED();
     return KNN_OK;
 }
@@ -1974,9 +2225,22 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     // Queries by cell (rows past the live count sort last), with a seed bound from their cell.
     if (T.tree)
         KNN_TRY(launch_descend(ix->dp, a.queries, ix->dims, nq, a.order, a.count_dev, T, a.k, k0, v0, seed, s));
-    else
-        KNN_TRY(launch_assign(ix->dp, a.queries, ix->dims, ix->dims, nq, a.order, a.count_dev, T.land.as<float>(), T.ps,
-                              T.cells, k0, v0, s, T.cell_far.as<float>(), T.cell_start.as<uint32_t>(), a.k, seed));
+    else {
+        // The rows' operand tiles in batch order, then the nearest landmark by the GEMM.
+        tc_pack_kernel<<<ceil_div(qrows, 128), 128, 0, s>>>(a.queries, ix->dims, ix->dims, a.order, nq, a.count_dev,
+                                                            kTileM, H, T.f16, T.scale, qimg, qnorm, 0.0f, nullptr, 0,
+                                                            nullptr, nullptr, qrows, nullptr);
+        KNN_LAUNCHED();
+        auto kern = H == 1 ? tc_assign_mma_kernel<1> : tc_assign_mma_kernel<2>;
+        const size_t smem = assign_mma_smem(H);
+        KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        kern<<<qtiles, 128, smem, s>>>(qimg, T.limg.as<uint8_t>(), T.lnorm.as<float>(), ceil_div(T.cells, kTileN),
+                                       T.cells, T.f16 ? idesc_f16(kTileM, kTileN) : idesc_bf16(kTileM, kTileN), nq,
+                                       a.order, a.count_dev, a.queries, ix->dims, T.land.as<float>(), T.ps,
+                                       T.cell_far.as<float>(), T.cell_start.as<uint32_t>(), a.k, k0, v0, seed,
+                                       reinterpret_cast<int*>(small + 1));
+        KNN_LAUNCHED();
+    }
     bool alt = false;
     KNN_TRY(radix_sort_pairs(k0, v0, k1, v1, nq, static_cast<int>(log2_ceil(T.cells + 1)), st, s, &alt));
     const uint32_t* cell_sorted = alt ? k1 : k0;

@@ -124,35 +124,6 @@ __device__ __forceinline__ void dist2_vec4_pair(const float (&q)[DP], const floa
     *db = acc_b;
 }
 
-// The same pair of distances with the query in shared memory (float4 broadcast reads).
-template <int DP>
-__device__ __forceinline__ void dist2_vec4_pair_sq(const float4* __restrict__ q4, const float4* __restrict__ pa,
-                                                   const float4* __restrict__ pb, float* da, float* db) {
-    static_assert(DP % 4 == 0, "vector path needs DP % 4 == 0");
-    float acc_a = 0.0f, acc_b = 0.0f;
-#pragma unroll
-    for (int v = 0; v < DP / 4; ++v) {
-        const float4 q = q4[v], x = pa[v], y = pb[v];
-        float t = __fsub_rn(q.x, x.x), u = __fsub_rn(q.x, y.x);
-        acc_a = __fmaf_rn(t, t, acc_a);
-        acc_b = __fmaf_rn(u, u, acc_b);
-        t = __fsub_rn(q.y, x.y);
-        u = __fsub_rn(q.y, y.y);
-        acc_a = __fmaf_rn(t, t, acc_a);
-        acc_b = __fmaf_rn(u, u, acc_b);
-        t = __fsub_rn(q.z, x.z);
-        u = __fsub_rn(q.z, y.z);
-        acc_a = __fmaf_rn(t, t, acc_a);
-        acc_b = __fmaf_rn(u, u, acc_b);
-        t = __fsub_rn(q.w, x.w);
-        u = __fsub_rn(q.w, y.w);
-        acc_a = __fmaf_rn(t, t, acc_a);
-        acc_b = __fmaf_rn(u, u, acc_b);
-    }
-    *da = acc_a;
-    *db = acc_b;
-}
-
 // Select q[dim] from a register array without dynamic indexing (which would force the array
 // into local memory).
 template <int DP>

@@ -179,10 +179,11 @@ struct knn_index {
     //   land   landmarks [cells][ps]; cell_start [cells + 1] first sorted point of each cell;
     //          cell_tile [cells + 1] first tile of each cell; cell_far [cells] float squared
     //          distance from each landmark to its farthest point
+    //   limg, lnorm  the landmarks as a 16-bit operand image and their scaled norms (+inf on padding)
     //   cimg, cdata, cmax  the cell centres as a 16-bit operand image, per centre tile their
     //          norms and radii (scaled), and an upper bound on the centres' norms
     struct TensorCoreState {
-        knn::DevBuf img, norm, pts, ids, pmax, land, cell_start, cell_tile, cell_far, cimg, cdata, cmax, ws;
+        knn::DevBuf img, norm, pts, ids, pmax, land, cell_start, cell_tile, cell_far, limg, lnorm, cimg, cdata, cmax, ws;
         // Tree layout (low dims): per tree node its split dimension, value and leaf cell (-1 for
         // splits); per cell its centre and radius (scaled) and box [2][bd] (scaled minima, maxima).
         knn::DevBuf node_dim, node_val, node_leaf, ccentre, cradius, box;

@@ -73,6 +73,19 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
         : "memory");
 }
 
+// ---- 16-byte asynchronous copy global -> shared, cached in L1 (cp.async.ca) ---------------------
+// Completion is tracked per thread in commit groups; after cp_async_wait<N>() the copies of all but
+// the newest N groups of this thread have landed, and a warp or block barrier publishes them to the
+// other threads.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // ---- tensor memory -------------------------------------------------------------------------------
 // Executed by one full warp.  The TMEM address is written to *slot (shared memory).
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
