@@ -3,6 +3,9 @@
 Default workload (the configuration the headline metric is quoted on): KdTreeGpu<3>,
 depthSkips 0, N = 4,194,304 points from a 64-component Gaussian mixture (sigma 0.01),
 Q = 1,048,576 queries from the same mixture, K = 16, max radius +inf; seeded synthetic data.
+Other workloads (`--workload`): c1, c3, c4, c5 (uneven batch) and `range`, the reference's
+range-limited speed test (N = 500,000 uniform points, Q = 10,000, K = 5, maxDistance2 = 0.01 D;
+`--dims 6..17`, `--structure kd|ball|bf`).
 
 One step = one exact query pass over the Q queries on the prebuilt tree (construction is timed
 once and reported separately).  Timed steps: CUDA events on the query stream, L2 flushed (a
@@ -52,7 +55,9 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "range"])
+    ap.add_argument("--dims", type=int, default=16, help="range workload: D in 6..17")
+    ap.add_argument("--structure", default="kd", choices=["kd", "ball", "bf"], help="range workload: index type")
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (debug only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-once", choices=["chosen", "plain"], default=None,
@@ -173,6 +178,8 @@ def max_over_ranks(world, value: float) -> float:
 
 
 def workload(args):
+    if args.workload == "range":
+        return W.range_limited(args.scale, args.dims, args.structure)
     return W.CONFIGS[args.workload](args.scale)
 
 
@@ -410,7 +417,7 @@ def run_reference(args, world, rank):
     threads = os.cpu_count() or 1
     import oracle
     kind = "port"
-    sample = {"c1": None, "c2": 262144, "c3": 4096, "c4": 64}[args.workload]
+    sample = {"c1": None, "c2": 262144, "c3": 4096, "c4": 64, "range": None}[args.workload]
     label = {"kd": "KdTree", "ball": "BallTree", "bf": "BruteForce"}[w.structure]
     if w.structure == "kd":
         tree = oracle.kd_tree(w.points, w.depth_skips)
@@ -601,7 +608,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": chosen_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, shapes of the config)",
         "config": {"workload": w.name, "structure": tree_kind_label(w), "n": int(w.points.shape[0]),
-                   "queries": count, "k": k, "depth_skips": w.depth_skips, "max_distance2": "inf",
+                   "queries": count, "k": k, "depth_skips": w.depth_skips,
+                   "max_distance2": "inf" if math.isinf(w.max_dist2) else w.max_dist2,
                    "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
         "exact_match": {"chosen": exact["chosen"], "plain": exact["plain"], "e2e": e2e_exact,
                         "sample_queries": int(len(sample))},
@@ -634,7 +642,7 @@ def main():
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        sample_q = {"c1": None, "c2": None, "c3": 16384, "c4": 256}[args.workload]
+        sample_q = {"c1": None, "c2": None, "c3": 16384, "c4": 256, "range": None}[args.workload]
         qps, build_s, nq = cpu_baseline(w, threads, sample_q)
         line["cpu_baseline"] = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
                                 "sample": f"{nq} of {count} queries, oracle port of the reference's CPU "

@@ -91,6 +91,8 @@ _SIGNATURES = {
     "knn_ball_create": [_vp, _u32, _u32, _u32, _u32, _vp, _pp],
     "knn_destroy": [_vp],
     "knn_index_get_info": [_vp, ctypes.POINTER(IndexInfo)],
+    "knn_index_serialize": [_vp, _vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t), _vp],
+    "knn_index_deserialize": [_vp, ctypes.c_size_t, _vp, _pp],
     "knn_query": [_vp, _vp, _u32, _f, _u32, _vp, _vp, ctypes.POINTER(QueryOpts), _vp],
     "knn_query_radii": [_vp, _vp, _u32, _vp, _u32, _vp, _vp, ctypes.POINTER(QueryOpts), _vp],
     "knn_query_host": [_vp, _vp, _u32, _f, _u32, _vp, _vp, ctypes.POINTER(QueryOpts), _vp],

@@ -89,6 +89,15 @@ class _Index:
             _lib.load().knn_destroy(self._h)
             self._h = ctypes.c_void_p()
 
+    def serialize(self, stream=None) -> bytes:
+        """The index (device arrays and any radius model) as bytes (knn_index_serialize)."""
+        lib = _lib.load()
+        size = ctypes.c_size_t()
+        _lib.check(lib.knn_index_serialize(self._h, None, 0, ctypes.byref(size), _stream_handle(stream)))
+        buf = ctypes.create_string_buffer(size.value)
+        _lib.check(lib.knn_index_serialize(self._h, buf, size.value, ctypes.byref(size), _stream_handle(stream)))
+        return buf.raw
+
     def __del__(self):
         try:
             self.close()
@@ -248,6 +257,21 @@ class BallTreeGpu(_Index):
         self.dims = int(p.shape[1])
         _lib.check(_lib.load().knn_ball_create(p.data_ptr(), n, self.dims, depth_skips, c_block_size,
                                                _stream_handle(stream), ctypes.byref(self._h)))
+
+
+def load_index(blob: bytes, stream=None) -> _Index:
+    """An index rebuilt from `_Index.serialize()` bytes on the current device (knn_index_deserialize)."""
+    h = ctypes.c_void_p()
+    buf = ctypes.create_string_buffer(bytes(blob), len(blob))
+    _lib.check(_lib.load().knn_index_deserialize(buf, len(blob), _stream_handle(stream), ctypes.byref(h)))
+    info = _lib.IndexInfo()
+    _lib.check(_lib.load().knn_index_get_info(h, ctypes.byref(info)))
+    cls = {_lib.BRUTE_FORCE: BruteForceGpu, _lib.KD_TREE: KdTreeGpu, _lib.BALL_TREE: BallTreeGpu}[info.structure]
+    ix = cls.__new__(cls)
+    _Index.__init__(ix)
+    ix._h = h
+    ix.dims = int(info.dims)
+    return ix
 
 
 class Batch:

@@ -22,6 +22,9 @@ Named configurations (seed = 1000 + configuration number):
           sigma 0.3), Q=65,536, K=100.
 * ``c5``  64 independent sets: N log-uniform in [1,024, 1,048,576], D from {3, 8, 32},
           K from {1, 10, 64}, uniform points, Q = N/8; k-d tree for D <= 8, ball tree for D = 32.
+* ``range``  the reference's range-limited speed test (tests/DimXSpeedTests.cu:10-58): N=500,000
+          uniform points in [0,1)^D, Q=10,000 uniform queries, K=5, maxDistance2 = 0.01 D, for D
+          in 6..17; k-d tree (depthSkips 3), ball tree (depthSkips 1) or brute force.
 """
 
 from __future__ import annotations
@@ -150,6 +153,16 @@ def c5_sets(scale: float = 1.0, count: int = 64) -> list[Workload]:
         out.append(Workload(f"c5_set{i}_{structure}{d}_n{n}_k{k}", structure, pts, qs, k, INF,
                             skips))
     return out
+
+
+def range_limited(scale: float = 1.0, dims: int = 16, structure: str = "kd") -> Workload:
+    if not 6 <= dims <= 17:
+        raise ValueError("the range-limited test sweeps D = 6..17")
+    rng = _rng(1100 + dims)
+    n, q = int(500000 * scale), int(10000 * scale)
+    skips = {"kd": 3, "ball": 1, "bf": 0}[structure]
+    return Workload(f"range_{structure}{dims}_n{n}_q{q}_k5", structure, uniform(rng, n, dims), uniform(rng, q, dims),
+                    5, 0.01 * dims, skips)
 
 
 def functionality(scale: float = 1.0) -> Workload:

@@ -159,6 +159,17 @@ KNN_API int knn_ball_create(const float* d_points, uint32_t n, uint32_t dims, ui
 KNN_API int knn_destroy(knn_index* index);
 KNN_API int knn_index_get_info(const knn_index* index, knn_index_info* out);
 
+/* ---- serialised indexes (no counterpart in the reference, whose trees live only in the class
+ *      instance's device arrays: src/KdTreeGpu.cuh:293-294, src/BallTreeGpu.cuh:461-462) -------- */
+/* Writes the index (its device arrays and any learned-radius model) to host memory.  With
+ * host_buf NULL, only *size is set (the bytes needed).  Synchronises `stream`. */
+KNN_API int knn_index_serialize(const knn_index* index, void* host_buf, size_t capacity, size_t* size,
+                                void* stream);
+/* Rebuilds an index on the current device from knn_index_serialize's bytes, without the
+ * construction kernels.  Rejects (KNN_ERR_INVALID_ARGUMENT) a blob whose magic, version, shape,
+ * array sizes or checksum do not match, before any device memory is used. */
+KNN_API int knn_index_deserialize(const void* host_buf, size_t size, void* stream, knn_index** out);
+
 /* ---- queries (device pointers; enqueued on `stream`, a cudaStream_t, NULL = legacy stream) -- */
 KNN_API int knn_query(knn_index* index, const float* d_queries, uint32_t count, float max_distance2,
               uint32_t k, int32_t* d_indexes, float* d_distances, const knn_query_opts* opts,

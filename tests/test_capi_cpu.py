@@ -74,3 +74,55 @@ def test_cpp_shim_headers_compile():
                         f"-I{os.path.join(ROOT, 'include')}", "-c", src, "-o", out],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+def _blob(structure=1, n=1000, dims=3, aux=3, skips=0, has_model=0, model_k=0, sizes=(0, 0, 0, 0, 0),
+          payload=b"", magic=b"CEKNNIX1", version=1, checksum=None):
+    import struct
+
+    def fnv(data):
+        h = 0xcbf29ce484222325
+        for b in data:
+            h ^= b
+            h = (h * 0x100000001b3) & 0xFFFFFFFFFFFFFFFF
+        return h
+    head = struct.pack("<8sI5I2I5QQ", magic, version, structure, n, dims, aux, skips, has_model, model_k, *sizes,
+                       fnv(payload) if checksum is None else checksum)
+    assert len(head) == 88
+    return head + payload
+
+
+@pytest.mark.parametrize("case", ["short", "magic", "version", "sizes", "total", "checksum", "skips", "aux", "model"])
+def test_deserialize_rejects_malformed_blobs_without_a_device(case):
+    """knn_index_deserialize validates the header, the array sizes the shape implies, the total
+    size and the checksum before it touches the device (a kd tree of n=1000, dims 3, skips 0:
+    1023 splits, 1024 leaf slots of 4 floats)."""
+    lib = _lib.load()
+    good = dict(structure=_lib.KD_TREE, n=1000, dims=3, aux=3, skips=0, sizes=(0, 4 * 1023, 4 * 1024 * 4, 0, 0))
+    payload = bytes(4 * 1023 + 16 * 1024)
+    kw = dict(good, payload=payload)
+    if case == "short":
+        blob = b"CEKNNIX1"
+    elif case == "magic":
+        blob = _blob(**dict(kw, magic=b"NOTANIDX"))
+    elif case == "version":
+        blob = _blob(**dict(kw, version=2))
+    elif case == "sizes":
+        blob = _blob(**dict(kw, sizes=(0, 4 * 1023, 4 * 1024 * 4 - 16, 0, 16)))
+    elif case == "total":
+        blob = _blob(**kw)[:-4]
+    elif case == "checksum":
+        blob = bytearray(_blob(**kw))
+        blob[100] ^= 1
+        blob = bytes(blob)
+    elif case == "skips":
+        blob = _blob(**dict(kw, skips=12))
+    elif case == "aux":
+        blob = _blob(**dict(kw, aux=4))
+    else:
+        blob = _blob(**dict(kw, has_model=1, model_k=16))
+    h = ctypes.c_void_p()
+    buf = ctypes.create_string_buffer(blob, len(blob))
+    assert lib.knn_index_deserialize(buf, len(blob), None, ctypes.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    assert not h.value
+    assert b"serialised index" in lib.knn_last_error()

@@ -272,3 +272,23 @@ def test_leaf_bucket_scan(structure, leaf_scan):
     for traversal in (0, 1):
         gu.assert_rows_equal(*gu.run(ix, qs, 9, leaf_scan=leaf_scan, traversal=traversal), *want,
                              what=f"{structure} leaf_scan={leaf_scan} traversal={traversal}")
+
+
+# ---- the reference's range-limited speed test shape (tests/DimXSpeedTests.cu:10-58) -------------
+
+@pytest.mark.parametrize("dims", [6, 11, 17])
+@pytest.mark.parametrize("structure", ["bf", "kd", "ball"])
+def test_range_limited(structure, dims):
+    """Uniform points, K=5, maxDistance2 = 0.01 D (many rows unfilled), kd depthSkips 3, ball 1;
+    the plain form with the reference benchmark's template choices and the autotuned form."""
+    from cudaexactknn_gb300 import _lib
+    w = W.range_limited(0.04, dims, structure)
+    want = _oracle(w.points, w.queries, w.k, w.max_dist2)
+    ix = gu.make_index(structure, w.points, w.depth_skips)
+    plain = {"kd": dict(block_size=32, shmem_stack=True),
+             "ball": dict(block_size=16, heap=True, shmem_tracking=True, shmem_stack=True),
+             "bf": dict(block_size=32)}[structure]
+    for kw in (plain, dict(flags=_lib.QF_AUTOTUNE)):
+        got = gu.run(ix, w.queries, w.k, w.max_dist2, **kw)
+        gu.assert_rows_equal(*got, *want, what=f"range {structure}{dims} {kw}")
+    ix.close()
