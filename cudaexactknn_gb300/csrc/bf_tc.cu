@@ -91,8 +91,20 @@ constexpr uint32_t kCentreBit = 0x80000000u;  // item code: a centre tile
 constexpr uint32_t kBoundary = 0xFFFFFFFEu;   // item code: centre tiles done, mask next
 constexpr uint32_t kEnd = 0xFFFFFFFDu;        // item code: no more items
 
-__host__ __device__ __forceinline__ uint32_t a_bytes(uint32_t h) { return h * kTileM * 128u; }
-__host__ __device__ __forceinline__ uint32_t b_bytes(uint32_t h) { return h * kTileN * 128u; }
+// Operand image layout code (the template parameter H of the GEMM kernels): 1 or 2 = that many
+// blocks of 64 elements in 128-byte rows (128-byte swizzle), for more than 32 dims; 32 or 64 = one
+// block of 16 or 32 elements in 32- or 64-byte rows (32- or 64-byte swizzle), for up to 16 or 32
+// dims, so that narrow data moves no zero padding.
+__host__ __device__ constexpr uint32_t ly_row_bytes(uint32_t ly) { return ly >= 32 ? ly : 128u; }
+__host__ __device__ constexpr uint32_t ly_blocks(uint32_t ly) { return ly >= 32 ? 1u : ly; }
+__host__ __device__ constexpr uint32_t ly_elems(uint32_t ly) { return ly_blocks(ly) * ly_row_bytes(ly) / 2; }
+__host__ __device__ __forceinline__ uint32_t a_bytes(uint32_t ly) { return ly_blocks(ly) * kTileM * ly_row_bytes(ly); }
+__host__ __device__ __forceinline__ uint32_t b_bytes(uint32_t ly) { return ly_blocks(ly) * kTileN * ly_row_bytes(ly); }
+// Descriptors of K step ks (16 elements) of a `rows`-row operand image at shared address base.
+__device__ __forceinline__ uint64_t ly_desc(uint32_t ly, uint32_t base, uint32_t rows, uint32_t ks) {
+    const uint32_t W = ly_row_bytes(ly), per = W / 32;
+    return desc_sw(base + (ks / per) * rows * W + (ks % per) * 32u, W);
+}
 
 // Constants of the GEMM bound (scaled units).
 struct Bounds {
@@ -359,11 +371,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 } else {
                     tc_fence_after();
                     const uint32_t b0 = smem_addr(s ? sB1 : sB0);
-                    for (uint32_t ks = 0; ks < p.ksteps; ++ks) {
-                        const uint32_t h = ks >> 2, kk = ks & 3;
-                        mma_f16kind(tmem + (ACC == 2 ? s * kTileN : 0u), desc_sw128(a0 + h * kTileM * 128u + kk * 32u),
-                                    desc_sw128(b0 + h * kTileN * 128u + kk * 32u), p.idesc, ks != 0);
-                    }
+                    for (uint32_t ks = 0; ks < p.ksteps; ++ks)
+                        mma_f16kind(tmem + (ACC == 2 ? s * kTileN : 0u), ly_desc(H, a0, kTileM, ks),
+                                    ly_desc(H, b0, kTileN, ks), p.idesc, ks != 0);
                     mma_commit(empty + s);
                     mma_commit(acc_full + s);
                     last_mma = i;
@@ -482,48 +492,54 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 const uint32_t base = item * kTileN;
                 float* stage = sStage + row;  // slot x at stage[x * kTileM]
                 auto chunk = [&](const uint32_t (&r)[32], uint32_t c) {
-                    // Per half chunk of 16 columns: the hit mask first, branch-free; then each
-                    // lane walks its own hits (lanes side by side), recording candidates and folding
-                    // their distance upper bounds into its heap (theta is refreshed once per half
-                    // chunk, which only keeps extra candidates).
+                    // The hit mask of all 32 columns first, branch-free, in four independent
+                    // partial masks; then, per half of 16 columns with hits, each lane walks its
+                    // own hits (lanes side by side), recording candidates and folding their
+                    // distance upper bounds into its heap.  A hit is tested again against the
+                    // current theta first (theta only rises as T falls; testing against an older,
+                    // lower theta only keeps extra candidates).
+                    uint32_t mp[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+                    for (uint32_t j4 = 0; j4 < 8; ++j4) {
+                        const float4 n4 = pn4[c * 8 + j4];
+                        const float nn[4] = {n4.x, n4.y, n4.z, n4.w};
+#pragma unroll
+                        for (uint32_t e = 0; e < 4; ++e) {
+                            const uint32_t j = j4 * 4 + e;
+                            mp[e] |= (__fmaf_ru(-a, nn[e], __uint_as_float(r[j])) >= theta) ? (1u << j) : 0u;
+                        }
+                    }
+                    const uint32_t mask = (mp[0] | mp[1]) | (mp[2] | mp[3]);
+                    if (mask == 0) return;
 #pragma unroll
                     for (uint32_t half = 0; half < 2; ++half) {
-                        uint32_t m = 0;
-#pragma unroll
-                        for (uint32_t j4 = 0; j4 < 4; ++j4) {
-                            const float4 n4 = pn4[c * 8 + half * 4 + j4];
-                            const float nn[4] = {n4.x, n4.y, n4.z, n4.w};
-#pragma unroll
-                            for (uint32_t e = 0; e < 4; ++e) {
-                                const uint32_t j = half * 16 + j4 * 4 + e;
-                                m |= (__fmaf_ru(-a, nn[e], __uint_as_float(r[j])) >= theta) ? (1u << j) : 0u;
-                            }
-                        }
+                        uint32_t m = (mask >> (16 * half)) & 0xFFFFu;
                         if (m == 0) continue;
                         // This lane's 16 sums go to shared memory so that its hits can be taken
                         // bit by bit (registers cannot be indexed at run time).
 #pragma unroll
                         for (uint32_t jj = 0; jj < 16; ++jj) stage[jj * kTileM] = __uint_as_float(r[half * 16 + jj]);
-                        bool moved = false;
                         while (m) {
-                            const uint32_t j = static_cast<uint32_t>(__ffs(m) - 1);
+                            const uint32_t jj = static_cast<uint32_t>(__ffs(m) - 1);
                             m &= m - 1u;
-                            const float vj = stage[(j - half * 16) * kTileM];
+                            const uint32_t j = half * 16 + jj;
+                            const float vj = stage[jj * kTileM];
+                            const float nj = rd[c * 32 + j];
+                            if (!(__fmaf_ru(-a, nj, vj) >= theta)) continue;
                             if (count < p.cap) {
                                 my_cand[count] = base + c * 32 + j;
                                 my_v[count] = vj;
                             }
                             ++count;
                             // Upper bound of this pair's float distance (scaled).
-                            const float hi = __fmaf_ru(-2.0f, vj, __fadd_ru(E2, __fmul_ru(up_n, __fadd_ru(nq, rd[c * 32 + j]))));
+                            const float hi = __fmaf_ru(-2.0f, vj, __fadd_ru(E2, __fmul_ru(up_n, __fadd_ru(nq, nj))));
                             const float u = __fmul_ru(fmaxf(hi, 0.0f), up_g);
                             if (u < T) {
                                 heap.replace_top(u);
                                 T = heap.at(0);
-                                moved = true;
+                                set_theta();
                             }
                         }
-                        if (moved) set_theta();
                     }
                 };
                 // (The TMEM loads and waits are warp-collective: the warp reconverges before each.)
@@ -566,20 +582,38 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                     uint32_t* sNeed = reinterpret_cast<uint32_t*>(sStage);  // [kEpiWarps][kMaskWords]
                     const uint32_t ew = warp - 2, mwords = (p.cells + 31) / 32;
                     const float one_m_g = __fsub_rd(1.0f, b.g);
-                    for (uint32_t w = 0; w < mwords; ++w) {
-                        uint32_t bits = sMask[w], need = 0;
-                        while (bits) {
-                            const uint32_t bit = static_cast<uint32_t>(__ffs(bits) - 1);
-                            bits &= bits - 1u;
-                            if (!good) continue;
-                            const float* bx = p.box + static_cast<size_t>(w * 32 + bit) * 2 * BD;
-                            float acc = 0.0f;
+                    // Squared distance from the query to cell c's box, rounded down (16-byte loads,
+                    // the same address in every lane).
+                    auto box_d2 = [&](uint32_t c) {
+                        const float4* bx = reinterpret_cast<const float4*>(p.box + static_cast<size_t>(c) * 2 * BD);
+                        float acc = 0.0f;
 #pragma unroll
-                            for (uint32_t d = 0; d < BD; ++d) {
-                                const float gap = fmaxf(fmaxf(__fsub_rd(__ldg(bx + d), qb[d]), __fsub_rd(qb[d], __ldg(bx + BD + d))), 0.0f);
+                        for (uint32_t v = 0; v < BD / 4; ++v) {
+                            const float4 lo4 = __ldg(bx + v), hi4 = __ldg(bx + BD / 4 + v);
+                            const float lo[4] = {lo4.x, lo4.y, lo4.z, lo4.w}, hi[4] = {hi4.x, hi4.y, hi4.z, hi4.w};
+#pragma unroll
+                            for (uint32_t e = 0; e < 4; ++e) {
+                                const float q = qb[4 * v + e];
+                                const float gap = fmaxf(fmaxf(__fsub_rd(lo[e], q), __fsub_rd(q, hi[e])), 0.0f);
                                 acc = __fmaf_rd(gap, gap, acc);
                             }
-                            if (!(__fsub_rd(__fmul_rd(acc, one_m_g), b.c4) > T)) need |= 1u << bit;
+                        }
+                        return acc;
+                    };
+                    for (uint32_t w = 0; w < mwords; ++w) {
+                        uint32_t bits = good ? sMask[w] : 0u, need = 0;
+                        // Two cells at a time at 16 dims (their loads and sums are independent;
+                        // at 32 dims the second box would not fit the register budget).
+                        while (bits) {
+                            const uint32_t b0 = static_cast<uint32_t>(__ffs(bits) - 1);
+                            bits &= bits - 1u;
+                            const bool two = BD <= 16 && bits != 0;
+                            const uint32_t b1 = two ? static_cast<uint32_t>(__ffs(bits) - 1) : b0;
+                            if (two) bits &= bits - 1u;
+                            const float d0 = box_d2(w * 32 + b0);
+                            const float d1 = two ? box_d2(w * 32 + b1) : d0;
+                            if (!(__fsub_rd(__fmul_rd(d0, one_m_g), b.c4) > T)) need |= 1u << b0;
+                            if (!(__fsub_rd(__fmul_rd(d1, one_m_g), b.c4) > T)) need |= 1u << b1;
                         }
                         need = __reduce_or_sync(0xFFFFFFFFu, need);
                         if (lane == 0) sNeed[ew * kMaskWords + w] = need;
@@ -985,13 +1019,13 @@ __global__ void tc_pack_kernel(const float* __restrict__ src, uint32_t src_strid
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= padded_rows) return;
     const uint32_t t = r / tile_rows, rr = r % tile_rows;
-    uint8_t* base = img + static_cast<size_t>(t) * H * tile_rows * 128u;
+    uint8_t* base = img + static_cast<size_t>(t) * ly_blocks(H) * tile_rows * ly_row_bytes(H);
     const bool live = r < (live_count ? *live_count : rows);
     const uint32_t sr = live ? (row_of ? row_of[r] : r) : kNone;
     const bool valid = sr != kNone;
     float acc = 0.0f;
     bool inf = false;
-    for (uint32_t k = 0; k < 64 * H; ++k) {
+    for (uint32_t k = 0; k < ly_elems(H); ++k) {
         const float x = (valid && k < dims) ? src[static_cast<size_t>(sr) * src_stride + k] : 0.0f;
         const float xs = x * scale;  // exact: scale is a power of two and the result stays finite
         acc = __fmaf_rn(xs, xs, acc);
@@ -1006,7 +1040,7 @@ __global__ void tc_pack_kernel(const float* __restrict__ src, uint32_t src_strid
             inf |= !(fabsf(back) <= FLT_MAX);
             bits = __bfloat16_as_ushort(h);
         }
-        *reinterpret_cast<uint16_t*>(base + sw128_offset(tile_rows, rr, k)) = bits;
+        *reinterpret_cast<uint16_t*>(base + sw_offset(ly_row_bytes(H), tile_rows, rr, k)) = bits;
         if (copy && k < copy_stride) copy[static_cast<size_t>(r) * copy_stride + k] = x;
     }
     const bool ok = !inf && acc <= FLT_MAX;
@@ -1448,7 +1482,8 @@ __global__ void tc_slot_keys_kernel(const float* __restrict__ leaf, uint32_t lea
     vals[i] = i;
 }
 
-// Self-test: one 128 x 256 x (64 H) tile through the same descriptors, written to global.
+// Self-test: one 128 x 256 tile over the layout's whole K extent through the same descriptors,
+// written to global.
 template <uint32_t H>
 __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __restrict__ qimg,
                                                              const uint8_t* __restrict__ pimg, uint32_t idesc,
@@ -1479,10 +1514,9 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
         bulk_copy_g2s(sB, pimg, b_bytes(H), bar);
         if (mbar_wait(bar, 0, abort)) {
             tc_fence_after();
-            for (uint32_t h = 0; h < H; ++h)
-                for (uint32_t kk = 0; kk < 4; ++kk)
-                    mma_f16kind(tmem, desc_sw128(smem_addr(sA) + h * kTileM * 128u + kk * 32u),
-                                desc_sw128(smem_addr(sB) + h * kTileN * 128u + kk * 32u), idesc, (h | kk) != 0);
+            for (uint32_t ks = 0; ks < ly_elems(H) / 16; ++ks)
+                mma_f16kind(tmem, ly_desc(H, smem_addr(sA), kTileM, ks), ly_desc(H, smem_addr(sB), kTileN, ks), idesc,
+                            ks != 0);
             mma_commit(bar + 1);
         } else {
             *abort = 1;
@@ -1526,7 +1560,8 @@ size_t filter_launch_smem(uint32_t H, uint32_t k) {
     return std::max<size_t>(filter_smem(H, k), accumulators(H, k) == 2 ? 120 * 1024 : 80 * 1024);
 }
 
-uint32_t halves(uint32_t dims) { return dims <= 64 ? 1u : 2u; }
+// Layout code of the operand images for `dims` dimensions (see ly_row_bytes).
+uint32_t halves(uint32_t dims) { return dims <= 16 ? 32u : dims <= 32 ? 64u : dims <= 64 ? 1u : 2u; }
 
 Bounds make_bounds(uint32_t dims, bool f16, float scale) {
     const double u = f16 ? std::ldexp(1.0, -11) : std::ldexp(1.0, -8);
@@ -1609,11 +1644,9 @@ __global__ void __launch_bounds__(128, 1) tc_assign_mma_kernel(
             if (!*abort && mbar_wait(bar + st, (t >> 1) & 1u, abort)) {
                 ++loads_done;
                 tc_fence_after();
-                for (uint32_t h = 0; h < H; ++h)
-                    for (uint32_t kk = 0; kk < 4; ++kk)
-                        mma_f16kind(tmem, desc_sw128(smem_addr(sA) + h * kTileM * 128u + kk * 32u),
-                                    desc_sw128(smem_addr(sB + st * b_bytes(H)) + h * kTileN * 128u + kk * 32u), idesc,
-                                    (h | kk) != 0);
+                for (uint32_t ks = 0; ks < ly_elems(H) / 16; ++ks)
+                    mma_f16kind(tmem, ly_desc(H, smem_addr(sA), kTileM, ks),
+                                ly_desc(H, smem_addr(sB + st * b_bytes(H)), kTileN, ks), idesc, ks != 0);
                 mma_commit(bar + 2);
                 ++commits;
             } else {
@@ -2231,6 +2264,7 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
                                                             kTileM, H, T.f16, T.scale, qimg, qnorm, 0.0f, nullptr, 0,
                                                             nullptr, nullptr, qrows, nullptr);
         KNN_LAUNCHED();
+        if (H != 1 && H != 2) return fail(KNN_ERR_UNSUPPORTED, "landmark layout at %u dims", ix->dims);
         auto kern = H == 1 ? tc_assign_mma_kernel<1> : tc_assign_mma_kernel<2>;
         const size_t smem = assign_mma_smem(H);
         KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
@@ -2292,10 +2326,13 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     const size_t smem = filter_launch_smem(H, a.k);
     const uint32_t acc = accumulators(H, a.k);
     void (*kern)(const TcParams) = nullptr;
-    if (T.tree && T.bd == 16) kern = acc == 1 ? tc_filter_kernel<1, 1, 16> : tc_filter_kernel<1, 2, 16>;
-    else if (T.tree) kern = acc == 1 ? tc_filter_kernel<1, 1, 32> : tc_filter_kernel<1, 2, 32>;
+    // Up to 32 dims (tree layout, boxes of 16 or 32 dims): 32- or 64-byte rows; beyond, 128-byte.
+    if (H == 32) kern = acc == 1 ? tc_filter_kernel<32, 1, 16> : tc_filter_kernel<32, 2, 16>;
+    else if (H == 64) kern = acc == 1 ? tc_filter_kernel<64, 1, 32> : tc_filter_kernel<64, 2, 32>;
     else if (H == 1) kern = acc == 1 ? tc_filter_kernel<1, 1, 0> : tc_filter_kernel<1, 2, 0>;
     else kern = acc == 1 ? tc_filter_kernel<2, 1, 0> : tc_filter_kernel<2, 2, 0>;
+    if ((H >= 32) != T.tree || (H == 32 && T.bd != 16) || (H == 64 && T.bd != 32))
+        return fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: layout %u for a %s layout", H, T.tree ? "tree" : "landmark");
     KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));
     kern<<<qtiles, kThreads, smem, s>>>(p);
@@ -2393,7 +2430,8 @@ int tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* bad) {
         tc_pack_kernel<<<2, 128>>>(dp, dims, dims, nullptr, pn, nullptr, kTileN, H, f16 != 0, 1.0f, pimg, pnm, 0.0f,
                                    nullptr, 0, nullptr, nullptr, pn, nullptr);
         const size_t smem = 1024 + ab + bb + 64;
-        auto kern = H == 1 ? tc_selftest_kernel<1> : tc_selftest_kernel<2>;
+        auto kern = H == 32 ? tc_selftest_kernel<32> : H == 64 ? tc_selftest_kernel<64> : H == 1 ? tc_selftest_kernel<1>
+                                                                                        : tc_selftest_kernel<2>;
         KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
         kern<<<1, 128, smem>>>(qimg, pimg, f16 ? idesc_f16(kTileM, kTileN) : idesc_bf16(kTileM, kTileN), out, err);
         KNN_LAUNCHED_N(3);

@@ -147,15 +147,16 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[32]) {
 }
 
 // ---- tcgen05.mma ---------------------------------------------------------------------------------
-// Shared-memory matrix descriptor for a K-major operand in the 128-byte swizzle layout: rows of
-// 128 bytes (64 16-bit elements), 8-row groups 1024 bytes apart (stride byte offset), swizzle mode 2.
-__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
+// Shared-memory matrix descriptor for a K-major operand in the W-byte swizzle layout (W = 32, 64
+// or 128): rows of W bytes, 8-row groups 8 W bytes apart (stride byte offset), swizzle mode 6, 4
+// or 2.  Consecutive K steps of 16 elements within a row start 32 bytes apart.
+__device__ __forceinline__ uint64_t desc_sw(uint32_t saddr, uint32_t W) {
     uint64_t d = 0;
     d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);  // start address, 16-byte units
-    d |= static_cast<uint64_t>(1) << 16;                   // leading byte offset (unused for this layout)
-    d |= static_cast<uint64_t>(1024 >> 4) << 32;           // stride byte offset
+    d |= static_cast<uint64_t>(1) << 16;                   // leading byte offset (unused for these layouts)
+    d |= static_cast<uint64_t>((8u * W) >> 4) << 32;       // stride byte offset
     d |= static_cast<uint64_t>(1) << 46;                   // descriptor version
-    d |= static_cast<uint64_t>(2) << 61;                   // 128-byte swizzle
+    d |= static_cast<uint64_t>(W == 128 ? 2u : (W == 64 ? 4u : 6u)) << 61;
     return d;
 }
 
@@ -191,13 +192,16 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                  : "memory");
 }
 
-// Byte offset of 16-bit element (row, k) inside a K-major 128-byte-swizzled operand image with
-// `rows` rows: the K extent is cut into 64-element halves of rows x 128 bytes each; within a
-// half, the 16-byte chunk c of row r sits at chunk position c ^ (r & 7).
-__host__ __device__ __forceinline__ uint32_t sw128_offset(uint32_t rows, uint32_t row, uint32_t k) {
-    const uint32_t half = k >> 6, kk = k & 63;
+// Byte offset of 16-bit element (row, k) inside a K-major operand image in the W-byte swizzle with
+// `rows` rows: the K extent is cut into blocks of W/2 elements of rows x W bytes each; within a
+// block, the 16-byte chunk c of row r sits at chunk position c ^ ((r / (128 / W)) mod (W / 16))
+// (the hardware XORs address bits 4.. with bits 7..).
+__host__ __device__ __forceinline__ uint32_t sw_offset(uint32_t W, uint32_t rows, uint32_t row, uint32_t k) {
+    const uint32_t per = W / 2;
+    const uint32_t blk = k / per, kk = k % per;
     const uint32_t chunk = kk >> 3, within = kk & 7;
-    return half * rows * 128u + row * 128u + ((chunk ^ (row & 7u)) << 4) + within * 2u;
+    const uint32_t shift = W == 128 ? 0u : (W == 64 ? 1u : 2u);
+    return blk * rows * W + row * W + ((chunk ^ ((row >> shift) & (W / 16 - 1))) << 4) + within * 2u;
 }
 
 }  // namespace tc

@@ -21,9 +21,11 @@ def _flags():
     return _lib.QF_BF16_FILTER
 
 
-@pytest.mark.parametrize("dims", [16, 40, 64, 100, 128])
+@pytest.mark.parametrize("dims", [3, 9, 16, 17, 24, 32, 40, 64, 100, 128])
 def test_tensor_core_selftest(dims):
-    """tcgen05.mma over one 128x256 tile matches exact products of the FP16 and BF16 inputs."""
+    """tcgen05.mma over one 128x256 tile matches exact products of the FP16 and BF16 inputs, in
+    each operand layout: 32-byte rows (dims <= 16), 64-byte rows (<= 32), 128-byte rows (one or
+    two blocks of 64)."""
     from cudaexactknn_gb300 import _lib
     err = ctypes.c_float()
     bad = ctypes.c_uint32()
