@@ -129,7 +129,7 @@ struct TcParams {
     const float* queries;        // the caller's queries (for the box test)
     uint32_t dims;
     float scale;
-    uint32_t cells, ctiles, nq, ksteps, idesc;
+    uint32_t cells, ctiles, nq, ksteps, idesc, idesc_half;  // instruction descriptors: N = 256, 128
     Bounds b;
     float s2, max_d2;
     const float* radii;          // per query index, or null
@@ -255,7 +255,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     uint64_t* acc_empty = bars + 6;   // [2] accumulator and row data drained by the epilogue
     uint64_t* a_full = bars + 8;      // query tile landed
     uint64_t* mask_ready = bars + 9;  // kept-cell mask complete
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 10);
+    // One accumulator (ACC = 1): each item's MMAs run in two halves of 128 columns, the low half
+    // signalled on acc_lo_full and handed back on acc_lo_empty, so that the next item's low half
+    // is computed while the epilogue reads this item's high half.
+    uint64_t* acc_lo_full = bars + 10;   // [2]
+    uint64_t* acc_lo_empty = bars + 12;  // [2]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 14);
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -278,6 +283,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
             mbar_init(empty + i, 1);
             mbar_init(acc_full + i, 1);
             mbar_init(acc_empty + i, kEpiWarps * 32);
+            mbar_init(acc_lo_full + i, 1);
+            mbar_init(acc_lo_empty + i, kEpiWarps * 32);
         }
         mbar_init(a_full, 1);
         mbar_init(mask_ready, kEpiWarps * 32);
@@ -352,7 +359,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         if (lane == 0) {
             // MMA issuer: one accumulator per item; markers pass through.
             const uint32_t a0 = smem_addr(sA);
-            uint32_t i = 0, last_mma = kNone;
+            uint32_t i = 0;
+            uint64_t* drain_bar = nullptr;  // the last commit's barrier and phase
+            uint32_t drain_par = 0;
             bool ok = mbar_wait(a_full, 0, abort);
             while (ok) {
                 const uint32_t s = i & 1;
@@ -360,23 +369,51 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 // that used it last: item i-2 (two accumulators) or i-1 (one).
                 const uint32_t prev = i - ACC;
                 if (!mbar_wait(full + s, (i >> 1) & 1, abort) ||
-                    (i >= ACC && !mbar_wait(acc_empty + (prev & 1), (prev >> 1) & 1, abort))) {
+                    (ACC == 2 && i >= ACC && !mbar_wait(acc_empty + (prev & 1), (prev >> 1) & 1, abort))) {
                     ok = false;
                     break;
                 }
                 const uint32_t code = sItem[s];
                 if (code == kBoundary || code == kEnd) {
                     mbar_arrive(empty + s);
+                    if constexpr (ACC == 1) mbar_arrive(acc_lo_full + s);
                     mbar_arrive(acc_full + s);
-                } else {
+                } else if constexpr (ACC == 2) {
                     tc_fence_after();
                     const uint32_t b0 = smem_addr(s ? sB1 : sB0);
                     for (uint32_t ks = 0; ks < p.ksteps; ++ks)
-                        mma_f16kind(tmem + (ACC == 2 ? s * kTileN : 0u), ly_desc(H, a0, kTileM, ks),
-                                    ly_desc(H, b0, kTileN, ks), p.idesc, ks != 0);
+                        mma_f16kind(tmem + s * kTileN, ly_desc(H, a0, kTileM, ks), ly_desc(H, b0, kTileN, ks), p.idesc,
+                                    ks != 0);
                     mma_commit(empty + s);
                     mma_commit(acc_full + s);
-                    last_mma = i;
+                    drain_bar = acc_full + s;
+                    drain_par = (i >> 1) & 1;
+                } else {
+                    // Low half (rows 0-127 of the point tile into columns 0-127) once the previous
+                    // item's low half is drained, then the high half once it is drained too.
+                    const uint32_t b0 = smem_addr(s ? sB1 : sB0);
+                    const uint32_t hb = b0 + 128u * ly_row_bytes(H);
+                    if (i >= 1 && !mbar_wait(acc_lo_empty + (prev & 1), (prev >> 1) & 1, abort)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    for (uint32_t ks = 0; ks < p.ksteps; ++ks)
+                        mma_f16kind(tmem, ly_desc(H, a0, kTileM, ks), ly_desc(H, b0, kTileN, ks), p.idesc_half, ks != 0);
+                    mma_commit(acc_lo_full + s);
+                    drain_bar = acc_lo_full + s;
+                    drain_par = (i >> 1) & 1;
+                    if (i >= 1 && !mbar_wait(acc_empty + (prev & 1), (prev >> 1) & 1, abort)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    for (uint32_t ks = 0; ks < p.ksteps; ++ks)
+                        mma_f16kind(tmem + 128u, ly_desc(H, a0, kTileM, ks), ly_desc(H, hb, kTileN, ks), p.idesc_half,
+                                    ks != 0);
+                    mma_commit(empty + s);
+                    mma_commit(acc_full + s);
+                    drain_bar = acc_full + s;
                 }
                 ++i;
                 if (code == kEnd) break;
@@ -385,7 +422,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 *abort = 1;
                 // The MMAs already issued finish before TMEM is released.
                 volatile int never = 0;
-                if (last_mma != kNone) mbar_wait(acc_full + (last_mma & 1), (last_mma >> 1) & 1, &never);
+                if (drain_bar) mbar_wait(drain_bar, drain_par, &never);
             }
         }
     } else {
@@ -429,16 +466,28 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         auto take = [&](uint32_t* code) -> bool {
             const uint32_t s = i & 1;
             // The TMEM loads that follow are warp-collective: the whole warp proceeds or leaves.
-            const bool got = mbar_wait(acc_full + s, (i >> 1) & 1, abort) && mbar_wait(full + s, (i >> 1) & 1, abort);
+            const bool got =
+                mbar_wait((ACC == 1 ? acc_lo_full : acc_full) + s, (i >> 1) & 1, abort) && mbar_wait(full + s, (i >> 1) & 1, abort);
             if (!__all_sync(0xFFFFFFFFu, got)) return false;
             tc_fence_after();
             *code = sItem[s];
             return true;
         };
-        auto release = [&]() {
+        // Hands the item's accumulator (and, with one accumulator, its low half when `marker`: a
+        // marker has no half-way point) and row data back.
+        auto release = [&](bool marker) {
             tc_fence_before();
+            if (ACC == 1 && marker) mbar_arrive(acc_lo_empty + (i & 1));
             mbar_arrive(acc_empty + (i & 1));
             ++i;
+        };
+        // One accumulator: the low 128 columns are read; hand them back and wait for the high half.
+        auto half_way = [&]() {
+            tc_fence_before();
+            mbar_arrive(acc_lo_empty + (i & 1));
+            const bool got = mbar_wait(acc_full + (i & 1), (i >> 1) & 1, abort);
+            if (!__all_sync(0xFFFFFFFFu, got)) *abort = 1;  // the next take() leaves
+            tc_fence_after();
         };
         auto process = [&](uint32_t item, bool centre) {
             const uint32_t s = i & 1;
@@ -478,7 +527,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                     chunk(ra, c);
                     __syncwarp();
                     tmem_wait_ld(rb);
-                    if (c + 2 < kTileN / 32) tmem_ld32_async(tcol + (c + 2) * 32, ra);
+                    if (c + 2 < kTileN / 32) {
+                        if (ACC == 1 && c + 2 == kTileN / 64) half_way();
+                        tmem_ld32_async(tcol + (c + 2) * 32, ra);
+                    }
                     chunk(rb, c + 1);
                     __syncwarp();
                     if (c + 2 < kTileN / 32) tmem_wait_ld(ra);
@@ -549,7 +601,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                     chunk(ra, c);
                     __syncwarp();
                     tmem_wait_ld(rb);
-                    if (c + 2 < kTileN / 32) tmem_ld32_async(tcol + (c + 2) * 32, ra);
+                    if (c + 2 < kTileN / 32) {
+                        if (ACC == 1 && c + 2 == kTileN / 64) half_way();
+                        tmem_ld32_async(tcol + (c + 2) * 32, ra);
+                    }
                     chunk(rb, c + 1);
                     __syncwarp();
                     if (c + 2 < kTileN / 32) tmem_wait_ld(ra);
@@ -573,7 +628,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
             }
             if (code == kEnd) break;
             if (code == kBoundary) {
-                release();
+                release(true);
                 if constexpr (BD > 0) {
                     // Box test of every cell the centre test kept: each query's exact distance to
                     // the cell's box, lower-bounded with directed rounding; a cell stays when some
@@ -626,7 +681,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 continue;
             }
             process(code & ~kCentreBit, (code & kCentreBit) != 0);
-            release();
+            release(false);
         }
         if (!ok) *abort = 1;
         if (!boundary_done) boundary();
@@ -1544,7 +1599,7 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
 
 size_t filter_smem(uint32_t H, uint32_t k) {
     return 1024 + a_bytes(H) + 2 * b_bytes(H) + 2 * kRowData * sizeof(float) + kMaskWords * sizeof(uint32_t) + 16 +
-           (kStage + static_cast<size_t>(k)) * kTileM * 4 + 10 * 8 + 8;
+           (kStage + static_cast<size_t>(k)) * kTileM * 4 + 14 * 8 + 8;
 }
 
 // The filter allocates all 512 TMEM columns, so a second resident block on the same SM would
@@ -2308,6 +2363,7 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     p.nq = nq;
     p.ksteps = ceil_div(ix->dims, 16);
     p.idesc = T.f16 ? idesc_f16(kTileM, kTileN) : idesc_bf16(kTileM, kTileN);
+    p.idesc_half = T.f16 ? idesc_f16(kTileM, kTileN / 2) : idesc_bf16(kTileM, kTileN / 2);
     p.b = make_bounds(ix->dims, T.f16, T.scale);
     p.s2 = T.scale * T.scale;
     p.max_d2 = a.max_d2;
