@@ -152,7 +152,7 @@ int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& p
     uint32_t* list_count = c.take<uint32_t>(1);
     void* scratch = c.take<uint8_t>(knn::retry_scratch_bytes(a.count));
     KNN_TRY(knn::model_predict(ix->model.as<float>(), ix->dims, a.queries, a.count, a.max_d2, a.radii, radii,
-                               nullptr, s));
+                               nullptr, s, true));
     knn::QueryArgs seeded = a;
     seeded.radii = radii;
     seeded.order = order;

@@ -271,7 +271,8 @@ size_t model_floats(uint32_t dims);
 int model_gradients(const float* d_prm, uint32_t dims, const float* d_x, const float* d_t, const uint32_t* d_rows,
                     uint32_t batch, float* d_grad, float* d_loss_rows, DevBuf& scratch, cudaStream_t s);
 int model_predict(const float* d_prm, uint32_t dims, const float* d_x, uint32_t count, float max_d2,
-                  const float* user_radii, float* d_radii, float* d_raw, cudaStream_t s);
+                  const float* user_radii, float* d_radii, float* d_raw, cudaStream_t s,
+                  bool tensor_cores = false);
 // Stable list (in `order`, or index order) of the queries that must be searched again, with
 // their seeded radii grown by `grow` (capped by the caller's radius).
 size_t retry_scratch_bytes(uint32_t count);

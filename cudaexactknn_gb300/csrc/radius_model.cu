@@ -19,6 +19,8 @@
 // Parameter layout (floats): W1[64][E] b1[64] W2[64][64] b2[64] w3[64] b3 (trainable), then the
 // fixed projection B[D][32], the scaling lo[D] inv_range[D], and the calibrated margin.
 
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -26,6 +28,7 @@
 #include <vector>
 
 #include "knn_internal.h"
+#include "tc_ptx.cuh"
 
 namespace knn {
 
@@ -365,9 +368,206 @@ int model_gradients(const float* d_prm, uint32_t dims, const float* d_x, const f
     return KNN_OK;
 }
 
-int model_predict(const float* d_prm, uint32_t dims, const float* d_x, uint32_t count, float max_d2,
-                  const float* user_radii, float* d_radii, float* d_raw, cudaStream_t s) {
+// ---- inference on the tensor cores ----------------------------------------------------------------
+// Seeded radii for a query batch (the query path, and the training margin, so that the margin is
+// measured on the same predictions): per 128-query tile, each thread builds its query's features
+// (scaled coordinates, sin/cos of the Fourier projections), rounds them to FP16 and writes them to
+// shared memory as the A operand (K-major, 128-byte swizzle); the hidden layers are tcgen05 GEMMs
+// against W1 (64 x F) and W2 (64 x 64), packed to FP16 in shared memory once per block, with FP32
+// accumulation in TMEM (columns 0-63 and 64-127); bias, ReLU and the output layer run in the
+// epilogue.  The prediction only seeds a radius that the fallback rounds correct, so the 16-bit
+// rounding changes no answer.  Blocks loop over tiles; every wait is bounded and a timeout leaves
+// the caller's radius (the unseeded search) for the rest of the block's rows.
+constexpr uint32_t kMlpRows = 128;
+constexpr uint32_t kMlpFeatMax = 128;  // features per row this kernel takes (dims <= 64)
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// FP16 element (row, k) of a K-major 128-byte-swizzled image with `rows` rows.
+__device__ __forceinline__ void put_half(uint8_t* img, uint32_t rows, uint32_t row, uint32_t k, float v) {
+    *reinterpret_cast<__half*>(img + tc::sw_offset(128, rows, row, k)) = __float2half_rn(fminf(fmaxf(v, -65504.0f), 65504.0f));
+}
+
+__device__ __forceinline__ uint64_t mlp_desc(uint32_t base, uint32_t rows, uint32_t ks) {
+    return tc::desc_sw(base + (ks / 4) * rows * 128u + (ks % 4) * 32u, 128);
+}
+
+template <int DP>
+__global__ void __launch_bounds__(kMlpRows, 1) mlp_infer_tc_kernel(const float* __restrict__ prm, uint32_t dims,
+                                                                   const float* __restrict__ x, uint32_t count,
+                                                                   float max_d2, const float* __restrict__ user_radii,
+                                                                   float* __restrict__ radii, float* __restrict__ raw) {
+    using namespace tc;
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw_a = smem_addr(smem_raw);
+    uint8_t* smem = smem_raw + (((raw_a + 1023u) & ~1023u) - raw_a);
+    uint8_t* sA1 = smem;                        // [128 rows][128 features] FP16, two 64-element blocks
+    uint8_t* sW1 = sA1 + kMlpRows * 256;        // [64 hidden][128 features]
+    uint8_t* sA2 = sW1 + kHidden * 256;         // [128 rows][64 hidden], one block
+    uint8_t* sW2 = sA2 + kMlpRows * 128;        // [64][64]
+    float* sb = reinterpret_cast<float*>(sW2 + kHidden * 128);  // b1[64], b2[64], w3[64]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sb + 3 * kHidden);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+    volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
     const ModelLayout L(dims);
+    const uint32_t t = threadIdx.x, warp = t / 32, lane = t % 32;
+    // Weights to FP16 images (zero beyond the features), biases and the output layer.
+    for (uint32_t e = t; e < kHidden * kMlpFeatMax; e += kMlpRows) {
+        const uint32_t n = e / kMlpFeatMax, f = e % kMlpFeatMax;
+        put_half(sW1, kHidden, n, f, f < L.feats ? prm[L.w1 + n * L.feats + f] : 0.0f);
+    }
+    for (uint32_t e = t; e < kHidden * kHidden; e += kMlpRows)
+        put_half(sW2, kHidden, e / kHidden, e % kHidden, prm[L.w2 + e]);
+    for (uint32_t e = t; e < kHidden; e += kMlpRows) {
+        sb[e] = prm[L.b1 + e];
+        sb[kHidden + e] = prm[L.b2 + e];
+        sb[2 * kHidden + e] = prm[L.w3 + e];
+    }
+    if (t == 0) {
+        mbar_init(bar, 1);
+        *abort = 0;
+        mbar_fence_init();
+    }
+    if (warp == 0) tmem_alloc(tmem_slot, 128);
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t idesc = idesc_f16(kMlpRows, kHidden);
+    const uint32_t k1 = (L.feats + 15) / 16;
+    const float b3 = prm[L.b3], margin = prm[L.margin];
+    uint32_t phase = 0, commits = 0;  // commits: thread 0's count
+    for (uint32_t tile = blockIdx.x; tile * kMlpRows < count; tile += gridDim.x) {
+        const uint32_t q = tile * kMlpRows + t;
+        const bool live = q < count;
+        // Features of this thread's row.
+        float z[DP];
+#pragma unroll
+        for (int d = 0; d < DP; ++d)
+            z[d] = (live && static_cast<uint32_t>(d) < dims)
+                       ? (x[static_cast<size_t>(q) * dims + d] - prm[L.lo + d]) * prm[L.inv_range + d] : 0.0f;
+#pragma unroll
+        for (int d = 0; d < DP; ++d)
+            if (static_cast<uint32_t>(d) < dims) put_half(sA1, kMlpRows, t, d, z[d]);
+        for (uint32_t f = 0; f < kFourier; ++f) {
+            float a = 0.0f;
+#pragma unroll
+            for (int d = 0; d < DP; ++d)
+                if (static_cast<uint32_t>(d) < dims) a = fmaf(z[d], prm[L.proj + d * kFourier + f], a);
+            float sv, cv;
+            sincospif(2.0f * a, &sv, &cv);
+            put_half(sA1, kMlpRows, t, dims + f, sv);
+            put_half(sA1, kMlpRows, t, dims + kFourier + f, cv);
+        }
+        for (uint32_t f = L.feats; f < kMlpFeatMax; ++f) put_half(sA1, kMlpRows, t, f, 0.0f);
+        fence_proxy_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+            tc_fence_after();
+            for (uint32_t ks = 0; ks < k1; ++ks)
+                mma_f16kind(tmem, mlp_desc(smem_addr(sA1), kMlpRows, ks), mlp_desc(smem_addr(sW1), kHidden, ks), idesc,
+                            ks != 0);
+            mma_commit(bar);
+            ++commits;
+        }
+        bool ok = !*abort && mbar_wait(bar, phase, abort);
+        phase ^= 1;
+        float h[kHidden];
+        if (__all_sync(0xFFFFFFFFu, ok)) {
+            tc_fence_after();
+            float v[32];
+            tmem_ld32(tmem + ((warp * 32u) << 16), v);
+#pragma unroll
+            for (uint32_t i = 0; i < 32; ++i) h[i] = fmaxf(v[i] + sb[i], 0.0f);
+            tmem_ld32(tmem + ((warp * 32u) << 16) + 32, v);
+#pragma unroll
+            for (uint32_t i = 0; i < 32; ++i) h[32 + i] = fmaxf(v[i] + sb[32 + i], 0.0f);
+        } else {
+            ok = false;
+            *abort = 1;
+#pragma unroll
+            for (uint32_t i = 0; i < kHidden; ++i) h[i] = 0.0f;
+        }
+#pragma unroll
+        for (uint32_t i = 0; i < kHidden; ++i) put_half(sA2, kMlpRows, t, i, h[i]);
+        fence_proxy_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0 && !*abort) {
+            tc_fence_after();
+            for (uint32_t ks = 0; ks < kHidden / 16; ++ks)
+                mma_f16kind(tmem + kHidden, mlp_desc(smem_addr(sA2), kMlpRows, ks), mlp_desc(smem_addr(sW2), kHidden, ks),
+                            idesc, ks != 0);
+            mma_commit(bar);
+            ++commits;
+        }
+        __syncthreads();
+        bool ok2 = !*abort && mbar_wait(bar, phase, abort);
+        phase ^= 1;
+        float y = b3;
+        if (__all_sync(0xFFFFFFFFu, ok2)) {
+            tc_fence_after();
+            float v[32];
+#pragma unroll
+            for (uint32_t c = 0; c < 2; ++c) {
+                tmem_ld32(tmem + ((warp * 32u) << 16) + kHidden + 32 * c, v);
+#pragma unroll
+                for (uint32_t i = 0; i < 32; ++i) y = fmaf(sb[2 * kHidden + 32 * c + i], fmaxf(v[i] + sb[kHidden + 32 * c + i], 0.0f), y);
+            }
+        } else {
+            ok2 = false;
+            *abort = 1;
+        }
+        if (live) {
+            const float cap = user_radii ? user_radii[q] : max_d2;
+            const bool good = ok && ok2;
+            if (raw) raw[q] = good ? y : INFINITY;
+            if (radii) radii[q] = good ? fminf(__expf(fminf(y + margin, 80.0f)), cap) : cap;
+        }
+        tc_fence_before();
+        __syncthreads();  // every read of sA1, sA2 and TMEM is done before the next tile's writes
+        if (*abort) break;
+    }
+    if (*abort && t == 0 && commits) {
+        // The MMAs already issued finish before TMEM is released.
+        volatile int never = 0;
+        mbar_wait(bar, (commits - 1) & 1, &never);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 128);
+    }
+}
+
+size_t mlp_tc_smem() { return 1024 + kMlpRows * 256 + kHidden * 256 + kMlpRows * 128 + kHidden * 128 + 3 * kHidden * 4 + 64; }
+
+int model_predict(const float* d_prm, uint32_t dims, const float* d_x, uint32_t count, float max_d2,
+                  const float* user_radii, float* d_radii, float* d_raw, cudaStream_t s, bool tensor_cores) {
+    const ModelLayout L(dims);
+    if (tensor_cores && L.feats <= kMlpFeatMax && count > 0) {
+        const size_t smem = mlp_tc_smem();
+        const uint32_t grid = std::min<uint32_t>(ceil_div(count, kMlpRows), 3u * static_cast<uint32_t>(sm_count()));
+#define KNN_INFER_TC(D_)                                                                                           \
+        if (dims <= D_) {                                                                                          \
+            KNN_TRY_CUDA(cudaFuncSetAttribute(mlp_infer_tc_kernel<D_>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                              static_cast<int>(smem)));                                            \
+            mlp_infer_tc_kernel<D_><<<grid, kMlpRows, smem, s>>>(d_prm, dims, d_x, count, max_d2, user_radii,      \
+                                                                 d_radii, d_raw);                                  \
+            KNN_LAUNCHED();                                                                                        \
+            return KNN_OK;                                                                                         \
+        }
+        KNN_INFER_TC(4)
+        KNN_INFER_TC(8)
+        KNN_INFER_TC(16)
+        KNN_INFER_TC(32)
+        KNN_INFER_TC(64)
+#undef KNN_INFER_TC
+    }
     const size_t smem = (static_cast<size_t>((L.total + 3) & ~3u) + kHidden * L.feats) * sizeof(float);
     const bool aligned = (L.w2 % 4) == 0;
 #define KNN_INFER(D_)                                                                                     \
@@ -497,7 +697,8 @@ int model_train(knn_index* ix, const float* d_samples, uint32_t count, uint32_t 
     KNN_TRY_CUDA(cudaMemcpyAsync(hl.data(), loss_rows, batch * 4, cudaMemcpyDeviceToHost, s));
 
     // 4. Margin: the `coverage` quantile of (target - prediction) over the samples.
-    KNN_TRY(model_predict(prm, dims, d_samples, count, INFINITY, nullptr, nullptr, dist, s));
+    // (with the query path's tensor-core inference, so that the margin covers its predictions)
+    KNN_TRY(model_predict(prm, dims, d_samples, count, INFINITY, nullptr, nullptr, dist, s, true));
     std::vector<float> pred(count);
     KNN_TRY_CUDA(cudaMemcpyAsync(pred.data(), dist, count * 4, cudaMemcpyDeviceToHost, s));
     KNN_TRY_CUDA(cudaStreamSynchronize(s));
