@@ -796,7 +796,7 @@ __device__ __forceinline__ float dist2_smem(const float4* __restrict__ q4, const
 // one of two shared-memory stages (the copies of step j + 1 are in flight while step j is scored),
 // each lane sums its own row in dimension order and the keys go to the warp's buffer; a full
 // buffer is sorted and trimmed to the k smallest keys.
-template <int PS>
+template <int PS, int S>
 __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const RescoreArgs a) {
     using Sh = RescoreShape<PS>;
     extern __shared__ __align__(16) uint8_t rs_smem[];
@@ -805,8 +805,8 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
     if (r >= (a.live_count ? *a.live_count : a.nq)) return;  // warp-uniform
     uint8_t* mine = rs_smem + static_cast<size_t>(w) * a.warp_bytes;
     float4* stage = reinterpret_cast<float4*>(mine);                                   // [2][32][kSlot]
-    float4* sq = reinterpret_cast<float4*>(mine + 2 * Sh::kStageBytes);               // [PS / 4]
-    uint64_t* buf = reinterpret_cast<uint64_t*>(mine + 2 * Sh::kStageBytes + PS * 4);  // [a.buf]
+    float4* sq = reinterpret_cast<float4*>(mine + S * Sh::kStageBytes);               // [PS / 4]
+    uint64_t* buf = reinterpret_cast<uint64_t*>(mine + S * Sh::kStageBytes + PS * 4);  // [a.buf]
     const uint32_t qi = a.order[r];
     const uint32_t cnt = a.cand_count[r];
     if (cnt > a.cap) {
@@ -887,25 +887,9 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
     bool need_c = lane < kept;
     uint32_t pos_c = need_c ? c[lane] : 0u;
     uint32_t id_c = need_c ? a.ids[pos_c] : 0u;
-    if (steps) stage_rows(0, __ballot_sync(0xFFFFFFFFu, need_c), pos_c);
-    for (uint32_t j = 0; j < steps; ++j) {
-        uint32_t pos_n = 0, id_n = 0;
-        bool need_n = false;
-        if (j + 1 < steps) {
-            need_n = 32 * (j + 1) + lane < kept;
-            if (need_n) {
-                pos_n = c[32 * (j + 1) + lane];
-                id_n = a.ids[pos_n];
-            }
-            stage_rows((j + 1) & 1, __ballot_sync(0xFFFFFFFFu, need_n), pos_n);
-        } else {
-            cp_async_commit();  // an empty group: the wait below always leaves the newest one
-        }
-        cp_async_wait<1>();
-        __syncwarp();  // every lane's copies of step j have landed
-        uint64_t key = ~0ull;
-        if (need_c) key = make_key(dist2_smem<PS>(sq, stage + (j & 1) * 32 * Sh::kSlot + lane * Sh::kSlot),
-                                   static_cast<int32_t>(id_c));
+    // Appends this lane's key (if below the limit) to the warp's buffer, sorting and trimming it
+    // to the k smallest first when it could overflow.
+    auto append = [&](uint64_t key) {
         if (m + 32 > a.buf) {
             // Sort and keep the k smallest (the rest cannot be in the answer).
             uint32_t n2 = 1;
@@ -919,10 +903,49 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
         const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, take);
         if (take) buf[m + __popc(ballot & ((1u << lane) - 1u))] = key;
         m += __popc(ballot);
-        __syncwarp();  // stage j & 1 is read before step j + 2's copies overwrite it
-        pos_c = pos_n;
-        id_c = id_n;
-        need_c = need_n;
+        __syncwarp();  // the stage is read before the next copies overwrite it
+    };
+    if constexpr (S == 2) {
+        // Two stages: the copies of step j + 1 are in flight while step j is summed.
+        if (steps) stage_rows(0, __ballot_sync(0xFFFFFFFFu, need_c), pos_c);
+        for (uint32_t j = 0; j < steps; ++j) {
+            uint32_t pos_n = 0, id_n = 0;
+            bool need_n = false;
+            if (j + 1 < steps) {
+                need_n = 32 * (j + 1) + lane < kept;
+                if (need_n) {
+                    pos_n = c[32 * (j + 1) + lane];
+                    id_n = a.ids[pos_n];
+                }
+                stage_rows((j + 1) & 1, __ballot_sync(0xFFFFFFFFu, need_n), pos_n);
+            } else {
+                cp_async_commit();  // an empty group: the wait below always leaves the newest one
+            }
+            cp_async_wait<1>();
+            __syncwarp();  // every lane's copies of step j have landed
+            uint64_t key = ~0ull;
+            if (need_c) key = make_key(dist2_smem<PS>(sq, stage + (j & 1) * 32 * Sh::kSlot + lane * Sh::kSlot),
+                                       static_cast<int32_t>(id_c));
+            append(key);
+            pos_c = pos_n;
+            id_c = id_n;
+            need_c = need_n;
+        }
+    } else {
+        // One stage (wide rows): more warps per SM hide the copies instead.
+        for (uint32_t j = 0; j < steps; ++j) {
+            if (j) {
+                need_c = 32 * j + lane < kept;
+                pos_c = need_c ? c[32 * j + lane] : 0u;
+                id_c = need_c ? a.ids[pos_c] : 0u;
+            }
+            stage_rows(0, __ballot_sync(0xFFFFFFFFu, need_c), pos_c);
+            cp_async_wait<0>();
+            __syncwarp();
+            uint64_t key = ~0ull;
+            if (need_c) key = make_key(dist2_smem<PS>(sq, stage + lane * Sh::kSlot), static_cast<int32_t>(id_c));
+            append(key);
+        }
     }
     cp_async_wait<0>();
     uint32_t n2 = 1;
@@ -2255,14 +2278,16 @@ int tc_prepare(knn_index* ix, cudaStream_t s) {
 
 template <int PS>
 static int rescore(RescoreArgs ra, uint32_t count, cudaStream_t s) {
+    // Rows of 128 floats: one stage per warp (about 19 KB with the buffer), one warp per block, so
+    // that ~11 warps fit an SM; narrower rows: two stages, four warps per block.
+    constexpr int S = PS >= 128 ? 1 : 2;
     ra.buf = rescore_buf(ra.k);
-    ra.warp_bytes = 2 * RescoreShape<PS>::kStageBytes + PS * 4 + ra.buf * 8;
-    // Two warps per block at the widest rows (about 36 KB of stages and buffer each), else four.
-    const uint32_t warps = ra.warp_bytes > 24576 ? 2 : kRescoreWarps;
+    ra.warp_bytes = S * RescoreShape<PS>::kStageBytes + PS * 4 + ra.buf * 8;
+    const uint32_t warps = S == 1 ? 1u : kRescoreWarps;
     const size_t smem = static_cast<size_t>(warps) * ra.warp_bytes;
-    KNN_TRY_CUDA(cudaFuncSetAttribute(tc_rescore_kernel<PS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    KNN_TRY_CUDA(cudaFuncSetAttribute(tc_rescore_kernel<PS, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(smem)));
-    tc_rescore_kernel<PS><<<ceil_div(count, warps), 32 * warps, smem, s>>>(ra);
+    tc_rescore_kernel<PS, S><<<ceil_div(count, warps), 32 * warps, smem, s>>>(ra);
     KNN_LAUNCHED();
     return KNN_OK;
 }
