@@ -130,6 +130,8 @@ struct TcParams {
     uint32_t dims;
     float scale;
     uint32_t cells, ctiles, nq, ksteps, idesc, idesc_half;  // instruction descriptors: N = 256, 128
+    uint32_t qtiles;             // query tiles; blocks take the ones past gridDim.x from tile_counter
+    uint32_t* tile_counter;      // zero before the launch
     Bounds b;
     float s2, max_d2;
     const float* radii;          // per query index, or null
@@ -224,7 +226,6 @@ struct TileSeq {
     }
 };
 
-__device__ __forceinline__ void epilogue_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(kEpiWarps * 32) : "memory"); }
 
 // ACC accumulators of kTileN TMEM columns: 2 lets the MMAs of the next tile run while the
 // epilogue drains this one (one block per SM); 1 leaves room for two blocks per SM, whose
@@ -260,22 +261,17 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     // is computed while the epilogue reads this item's high half.
     uint64_t* acc_lo_full = bars + 10;   // [2]
     uint64_t* acc_lo_empty = bars + 12;  // [2]
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 14);
+    uint64_t* a_empty = bars + 14;       // the MMAs of a query tile are done with its operand
+    uint64_t* epi_bar = bars + 15;       // the epilogue warps' own barrier (bounded waits)
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 16);
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const uint32_t live_rows = p.live_count ? *p.live_count : p.nq;
-    const uint32_t qt = blockIdx.x;
-    if (qt * kTileM >= live_rows) return;  // whole block idle: leave before any allocation
-    TileSeq seq;
-    seq.t0 = p.qhome[4 * qt];
-    seq.t1 = p.qhome[4 * qt + 1];
-    seq.c0 = p.qhome[4 * qt + 2];
-    seq.c1 = p.qhome[4 * qt + 3];
-    seq.cells = p.cells;
-    seq.ctiles = p.ctiles;
-    seq.mask = sMask;
-    seq.cell_tile = p.cell_tile;
+    // The block's first query tile; later ones come from tile_counter, taken by the producer and
+    // passed to the other roles with each tile's end marker.
+    const uint32_t qt0 = blockIdx.x;
+    if (qt0 * kTileM >= live_rows) return;  // whole block idle: leave before any allocation
     for (uint32_t w = threadIdx.x; w < kMaskWords; w += blockDim.x) sMask[w] = 0;
     if (threadIdx.x == 0) {
         for (int i = 0; i < 2; ++i) {
@@ -287,6 +283,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
             mbar_init(acc_lo_empty + i, kEpiWarps * 32);
         }
         mbar_init(a_full, 1);
+        mbar_init(a_empty, 1);
+        mbar_init(epi_bar, kEpiWarps * 32);
         mbar_init(mask_ready, kEpiWarps * 32);
         *abort = 0;
         mbar_fence_init();
@@ -302,9 +300,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     // the MMA issuer and the epilogue take the items from there, in order.
     if (warp == 0) {
         if (lane == 0) {
-            mbar_expect_tx(a_full, a_bytes(H));
-            bulk_copy_g2s(sA, p.qimg + static_cast<size_t>(qt) * a_bytes(H), a_bytes(H), a_full);
-            uint32_t issued = 0, data_tiles = 0;
+            uint32_t issued = 0, data_tiles = 0, tiles = 0, a_loads = 0;
             auto stage_free = [&](uint32_t s) -> bool {
                 // Stage s is free once the MMAs of item issued-2 are done (operands) and the
                 // epilogue has drained it (row data).
@@ -328,28 +324,61 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 data_tiles += centre ? 0u : 1u;
                 return true;
             };
-            auto marker = [&](uint32_t code) -> bool {
+            // A marker item; `meta` travels in the stage's sMeta slot (the next tile, for kEnd).
+            auto marker = [&](uint32_t code, uint32_t meta) -> bool {
                 const uint32_t s = issued & 1;
                 if (!stage_free(s)) return false;
                 sItem[s] = code;
+                sMeta[s] = __uint_as_float(meta);
                 mbar_arrive(full + s);
                 ++issued;
                 return true;
             };
             bool ok = true;
-            uint32_t item;
-            bool centre;
-            for (uint32_t st = 0; ok && st < 3; ++st) {
-                if (st == 2) ok = marker(kBoundary) && mbar_wait(mask_ready, 0, abort) && !*abort;
-                seq.begin(st);
-                while (ok && seq.next(&item, &centre)) ok = load(item, centre);
+            for (uint32_t qt = qt0;;) {
+                // The query tile's operand, once the MMAs of the block's previous tile are done.
+                if (tiles > 0 && !mbar_wait(a_empty, (tiles - 1) & 1, abort)) {
+                    ok = false;
+                    break;
+                }
+                mbar_expect_tx(a_full, a_bytes(H));
+                bulk_copy_g2s(sA, p.qimg + static_cast<size_t>(qt) * a_bytes(H), a_bytes(H), a_full);
+                ++a_loads;
+                // (The kept-cell mask of the previous tile was read to the end; the epilogue writes
+                // this tile's only after the centre items below.)
+                if (tiles > 0)
+                    for (uint32_t w = 0; w < kMaskWords; ++w) sMask[w] = 0;
+                TileSeq seq;
+                seq.t0 = p.qhome[4 * qt];
+                seq.t1 = p.qhome[4 * qt + 1];
+                seq.c0 = p.qhome[4 * qt + 2];
+                seq.c1 = p.qhome[4 * qt + 3];
+                seq.cells = p.cells;
+                seq.ctiles = p.ctiles;
+                seq.mask = sMask;
+                seq.cell_tile = p.cell_tile;
+                uint32_t item;
+                bool centre;
+                for (uint32_t st = 0; ok && st < 3; ++st) {
+                    if (st == 2) ok = marker(kBoundary, 0) && mbar_wait(mask_ready, tiles & 1, abort) && !*abort;
+                    seq.begin(st);
+                    while (ok && seq.next(&item, &centre)) ok = load(item, centre);
+                }
+                uint32_t next = kNone;
+                if (ok) {
+                    const uint32_t t = gridDim.x + atomicAdd(p.tile_counter, 1u);
+                    if (t < p.qtiles && t * kTileM < live_rows) next = t;
+                }
+                ok = ok && marker(kEnd, next);
+                ++tiles;
+                if (!ok || next == kNone) break;
+                qt = next;
             }
-            ok = ok && marker(kEnd);
             if (!ok) {
                 *abort = 1;
                 // Let copies in flight land before the block can exit.
                 volatile int never = 0;
-                mbar_wait(a_full, 0, &never);
+                if (a_loads) mbar_wait(a_full, (a_loads - 1) & 1, &never);
                 for (uint32_t i = issued >= 2 ? issued - 2 : 0; i < issued; ++i)
                     mbar_wait(full + (i & 1), (i >> 1) & 1, &never);
             }
@@ -359,10 +388,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         if (lane == 0) {
             // MMA issuer: one accumulator per item; markers pass through.
             const uint32_t a0 = smem_addr(sA);
-            uint32_t i = 0;
+            uint32_t i = 0, tiles = 0, next = kNone;
             uint64_t* drain_bar = nullptr;  // the last commit's barrier and phase
             uint32_t drain_par = 0;
-            bool ok = mbar_wait(a_full, 0, abort);
+            bool ok = true;
+            for (;;) {
+            ok = mbar_wait(a_full, tiles & 1, abort);
             while (ok) {
                 const uint32_t s = i & 1;
                 // The accumulator this item writes is free once the epilogue has drained the item
@@ -375,6 +406,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 }
                 const uint32_t code = sItem[s];
                 if (code == kBoundary || code == kEnd) {
+                    if (code == kEnd) {
+                        next = __float_as_uint(sMeta[s]);  // read before the stage is handed back
+                        mma_commit(a_empty);  // the query operand is free once this tile's MMAs are done
+                    }
                     mbar_arrive(empty + s);
                     if constexpr (ACC == 1) mbar_arrive(acc_lo_full + s);
                     mbar_arrive(acc_full + s);
@@ -418,6 +453,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 ++i;
                 if (code == kEnd) break;
             }
+            if (!ok) break;
+            ++tiles;
+            if (next == kNone) break;
+            }
             if (!ok) {
                 *abort = 1;
                 // The MMAs already issued finish before TMEM is released.
@@ -429,6 +468,16 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         // Epilogue: thread = query row.  TMEM lanes 32*(warp%4) .. +31 belong to this warp.
         const uint32_t quarter = warp & 3;
         const uint32_t row = quarter * 32 + lane;
+        uint32_t i = 0;  // items taken, over all of the block's tiles
+        // The four epilogue warps meet here (an mbarrier with the kernel's bounded wait rather than
+        // a named barrier, so that a warp that gives up cannot leave the others waiting forever).
+        uint32_t epi_phase = 0;
+        auto epi_sync = [&]() {
+            mbar_arrive(epi_bar);
+            mbar_wait(epi_bar, epi_phase & 1, abort);
+            ++epi_phase;
+        };
+        for (uint32_t qt = qt0;;) {
         const uint32_t r = qt * kTileM + row;  // row of the sorted batch
         const bool live = r < live_rows;
         const uint32_t qi = live ? p.order[r] : 0u;
@@ -442,7 +491,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         const float r2 = fminf(p.radii ? fminf(p.radii[qi], p.max_d2) : p.max_d2, p.seed[qi]);
         const float seed = good ? __fmul_ru(r2, p.s2) : 0.0f;
         BoundHeap heap{heap_base + row, p.k};
-        for (uint32_t i = 0; i < p.k; ++i) heap.at(i) = seed;
+        for (uint32_t x = 0; x < p.k; ++x) heap.at(x) = seed;
         float T = seed;
         const float qup = good ? __fsqrt_ru(__fmul_ru(nq, __fadd_ru(1.0f, b.gn))) : 0.0f;  // >= |q'|
         const float one_m_gn = __fsub_rd(1.0f, b.gn);
@@ -461,7 +510,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         uint32_t* my_cand = p.cand + static_cast<size_t>(live ? r : 0) * p.cap;
         float* my_v = p.cand_v + static_cast<size_t>(live ? r : 0) * p.cap;
         const uint32_t taddr_row = tmem + ((quarter * 32u) << 16);
-        uint32_t i = 0;
         // Takes the next item (waits for its accumulator and row data); false on failure.
         auto take = [&](uint32_t* code) -> bool {
             const uint32_t s = i & 1;
@@ -615,8 +663,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         // epilogue warps complete the kept-cell mask and release the producer into phase 2.  A
         // warp that fails still joins that barrier (once) before it leaves.
         bool ok = true, boundary_done = false;
+        uint32_t next = kNone;
         auto boundary = [&]() {
-            epilogue_barrier();
+            epi_sync();
             mbar_arrive(mask_ready);
             boundary_done = true;
         };
@@ -626,14 +675,18 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 ok = false;
                 break;
             }
-            if (code == kEnd) break;
+            if (code == kEnd) {
+                next = __float_as_uint(sMeta[i & 1]);
+                release(true);
+                break;
+            }
             if (code == kBoundary) {
                 release(true);
                 if constexpr (BD > 0) {
                     // Box test of every cell the centre test kept: each query's exact distance to
                     // the cell's box, lower-bounded with directed rounding; a cell stays when some
                     // query may need it.
-                    epilogue_barrier();  // the centre test's mask is complete
+                    epi_sync();  // the centre test's mask is complete
                     uint32_t* sNeed = reinterpret_cast<uint32_t*>(sStage);  // [kEpiWarps][kMaskWords]
                     const uint32_t ew = warp - 2, mwords = (p.cells + 31) / 32;
                     const float one_m_g = __fsub_rd(1.0f, b.g);
@@ -673,7 +726,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                         need = __reduce_or_sync(0xFFFFFFFFu, need);
                         if (lane == 0) sNeed[ew * kMaskWords + w] = need;
                     }
-                    epilogue_barrier();
+                    epi_sync();
                     for (uint32_t w = threadIdx.x - 64; w < mwords; w += kEpiWarps * 32)
                         sMask[w] &= sNeed[w] | sNeed[kMaskWords + w] | sNeed[2 * kMaskWords + w] | sNeed[3 * kMaskWords + w];
                 }
@@ -688,6 +741,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         if (live) {
             p.cand_count[r] = (ok && good) ? count : kNone;
             p.final_t[r] = (ok && good) ? T : INFINITY;
+        }
+        if (!ok || next == kNone) break;
+        qt = next;
         }
     }
     tc_fence_before();
@@ -1622,7 +1678,7 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
 
 size_t filter_smem(uint32_t H, uint32_t k) {
     return 1024 + a_bytes(H) + 2 * b_bytes(H) + 2 * kRowData * sizeof(float) + kMaskWords * sizeof(uint32_t) + 16 +
-           (kStage + static_cast<size_t>(k)) * kTileM * 4 + 14 * 8 + 8;
+           (kStage + static_cast<size_t>(k)) * kTileM * 4 + 16 * 8 + 8;
 }
 
 // The filter allocates all 512 TMEM columns, so a second resident block on the same SM would
@@ -2332,7 +2388,7 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     float* seed = c.take<float>(nq);
     float* retry_r2 = c.take<float>(nq);
     uint64_t* xkeys = c.take<uint64_t>(static_cast<size_t>(nq) * kExhChunks * a.k);
-    uint32_t* small = c.take<uint32_t>(64);  // [0] retry count, [1] error flag
+    uint32_t* small = c.take<uint32_t>(64);  // [0] retry count, [1] error flag, [2] filter tile counter
     KNN_TRY_CUDA(cudaMemsetAsync(small, 0, 64 * sizeof(uint32_t), s));
 
     // Queries by cell (rows past the live count sort last), with a seed bound from their cell.
@@ -2404,8 +2460,16 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     p.final_t = final_t;
     p.counters = a.counters;
     p.error = reinterpret_cast<int*>(small + 1);
+    p.qtiles = qtiles;
+    p.tile_counter = small + 2;
+    // Rows no block settles (a block that gave up) keep these: the plain search within a huge radius.
+    KNN_TRY_CUDA(cudaMemsetAsync(cnt, 0xFF, nq * 4ull, s));
+    KNN_TRY_CUDA(cudaMemsetAsync(final_t, 0x7F, nq * 4ull, s));
     const size_t smem = filter_launch_smem(H, a.k);
     const uint32_t acc = accumulators(H, a.k);
+    // Persistent blocks (one or two per SM, as TMEM allows) take query tiles in turn, so that
+    // tiles of uneven cost balance across the SMs instead of leaving a partial last wave.
+    const uint32_t grid = std::min<uint32_t>(qtiles, (acc == 2 ? 1u : 2u) * static_cast<uint32_t>(sm_count()));
     void (*kern)(const TcParams) = nullptr;
     // Up to 32 dims (tree layout, boxes of 16 or 32 dims): 32- or 64-byte rows; beyond, 128-byte.
     if (H == 32) kern = acc == 1 ? tc_filter_kernel<32, 1, 16> : tc_filter_kernel<32, 2, 16>;
@@ -2416,7 +2480,7 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
         return fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: layout %u for a %s layout", H, T.tree ? "tree" : "landmark");
     KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));
-    kern<<<qtiles, kThreads, smem, s>>>(p);
+    kern<<<grid, kThreads, smem, s>>>(p);
     KNN_LAUNCHED();
     if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
 
