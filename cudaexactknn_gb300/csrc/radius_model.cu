@@ -2,11 +2,13 @@
 // query's coordinates, the logarithm of its k-th neighbour's squared distance.  The prediction
 // plus a calibrated margin seeds each query's search radius (max_distance2); a query that finds
 // fewer than k points inside its seeded radius is searched again without the seed, so answers
-// stay exact and the plain search is both the fallback and the judge.
+// stay exact and the plain search is both the fallback and the arbiter.
 //
 // Training runs on the GPU with the kernels below (forward + backward per sample, weight
 // gradients as batch reductions in a fixed order, Adam), on targets produced by the engine's own
-// exact search for sample queries.  The reference has no counterpart: its pruning radius is the
+// exact search for sample queries.  Query-time inference runs on the tensor cores
+// (mlp_infer_tc_kernel, FP16 operands, FP32 accumulation); the prediction API keeps the FP32
+// kernel.  The reference has no counterpart: its pruning radius is the
 // caller's single Query::maxDistance2 (src/KnnTrees.cuh:228, used at src/KdTreeGpu.cuh:211 and
 // src/BallTreeGpu.cuh:48).
 //
