@@ -144,3 +144,22 @@ def test_queries_outside_the_format_fall_back():
     gu.assert_rows_equal(*gu.run(ix, qs, 10, flags=_flags()), *want, what="fp16 overflow queries")
     c = ix.stats(knn.Query(gu.to_dev(qs), len(qs), float("inf")), 10, flags=_flags())
     assert c.fallback_queries == len(range(0, 300, 7))
+
+
+@pytest.mark.parametrize("structure,dims,k,nq", [("bf", 128, 100, 24000), ("ball", 16, 32, 48000), ("bf", 64, 10, 48000)])
+def test_persistent_blocks_take_several_query_tiles(structure, dims, k, nq):
+    """More 128-query tiles than resident filter blocks (one per SM with two accumulators, two with
+    one), so blocks take further tiles from the counter; a sample of rows against the oracle."""
+    rng = np.random.default_rng(dims + k)
+    if structure == "ball":
+        pts, basis = W.subspace(rng, 20000, dims, 4, 0.05)
+        qs, _ = W.subspace(rng, nq, dims, 4, 0.05, basis)
+    else:
+        pts, centres = W.gauss_mix(rng, 20000, dims, 32, 0.3)
+        qs, _ = W.gauss_mix(rng, nq, dims, 32, 0.3, centres)
+    ix = gu.make_index(structure, pts, 1 if structure == "ball" else None)
+    idx, dist = gu.run(ix, qs, k, flags=_flags())
+    rows = np.random.default_rng(1).choice(nq, size=1500, replace=False)
+    want = oracle.bf_knn(pts, qs[rows], k, fma=True, threads=8)
+    gu.assert_rows_equal(idx[rows], dist[rows], *want, what=f"{structure} D={dims} k={k} nq={nq}")
+    ix.close()
