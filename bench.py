@@ -155,10 +155,19 @@ def dist_setup():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
-        backend = "nccl"
-        dist.init_process_group(backend)
+        # NCCL between GPUs; gloo where there is none (the reference arm and the rank helpers
+        # need no device).
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return world, rank, local
+
+
+def dist_teardown(world):
+    if world > 1:
+        import torch.distributed as dist
+        if dist.is_initialized():
+            dist.destroy_process_group()
 
 
 def barrier(world):
@@ -172,7 +181,8 @@ def max_over_ranks(world, value: float) -> float:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -653,4 +663,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    try:
+        main()
+    finally:
+        dist_teardown(int(os.environ.get("WORLD_SIZE", "1")))
