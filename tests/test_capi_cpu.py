@@ -126,3 +126,47 @@ def test_deserialize_rejects_malformed_blobs_without_a_device(case):
     assert lib.knn_index_deserialize(buf, len(blob), None, ctypes.byref(h)) == _lib.ERR_INVALID_ARGUMENT
     assert not h.value
     assert b"serialised index" in lib.knn_last_error()
+
+
+def _header_prototypes():
+    import re
+    text = open(_lib.HEADER).read()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    protos = {}
+    for name, params in re.findall(r"KNN_API\s+[\w\s\*]+?\b(knn_\w+)\s*\(([^)]*)\)", text, flags=re.S):
+        params = params.strip()
+        protos[name] = 0 if params in ("", "void") else len(params.split(","))
+    return protos
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every declared function has a ctypes signature with the header's parameter count, so a
+    Python caller can never pass a misaligned argument list."""
+    protos = _header_prototypes()
+    assert set(protos) == set(_lib.header_symbols())
+    assert set(protos) == set(_lib._SIGNATURES), set(protos) ^ set(_lib._SIGNATURES)
+    for name, count in protos.items():
+        assert len(_lib._SIGNATURES[name]) == count, name
+
+
+def test_ctypes_structs_match_the_c_layout(tmp_path):
+    """The Python mirrors of the header's structs have the C compiler's size and field offsets."""
+    structs = {"knn_query_opts": _lib.QueryOpts, "knn_query_counters": _lib.QueryCounters,
+               "knn_index_info": _lib.IndexInfo, "knn_train_opts": _lib.TrainOpts,
+               "knn_train_report": _lib.TrainReport, "knn_batch_item": _lib.BatchItem}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "cudaexactknn.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{os.path.join(ROOT, 'include')}", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    got = {tuple(line.split()[:2]): int(line.split()[2]) for line in out.splitlines()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
