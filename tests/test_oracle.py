@@ -138,3 +138,47 @@ def test_radius_model_reference_gradient_is_consistent():
         h[i] = 1e-5
         num = (ref.loss_and_grad(p + h, d, x, t)[0] - ref.loss_and_grad(p - h, d, x, t)[0]) / 2e-5
         assert abs(g[i] - num) <= 1e-6 * max(1.0, abs(num))
+
+
+REF_PAIRS = [(1, 4), (2, 5), (3, 1), (3, 8), (3, 16), (4, 10), (5, 10), (8, 5), (8, 10), (16, 32), (32, 64)]
+
+
+@pytest.mark.parametrize("dims,k", REF_PAIRS)
+@pytest.mark.parametrize("seed", [11, 12])
+def test_oracle_matches_the_reference_build_on_fresh_seeds(dims, k, seed):
+    """Beyond the committed vectors: the reference's own CPU classes (oracle/_ref, built from its
+    sources where they are mounted) and the restatement agree on fresh seeded data, every
+    structure, several depthSkips, both tracking modes, with and without a radius.  Skipped where
+    oracle/_ref is absent (it is built for this machine only)."""
+    if not (oracle.ref_available(False) and oracle.ref_available(True)):
+        pytest.skip("oracle/_ref not built on this machine")
+    rng = np.random.default_rng(seed * 1000 + dims * 10 + k)
+    n = int(rng.integers(k, 3000))
+    if seed % 2:
+        pts = rng.random((n, dims), dtype=np.float32)
+        qs = rng.random((200, dims), dtype=np.float32)
+    else:
+        centres = rng.random((8, dims))
+        pts = (centres[rng.integers(0, 8, n)] + 0.02 * rng.standard_normal((n, dims))).astype(np.float32)
+        qs = (centres[rng.integers(0, 8, 200)] + 0.02 * rng.standard_normal((200, dims))).astype(np.float32)
+    r2_small = float(np.float32(0.05 * dims * (0.02 if seed % 2 == 0 else 0.2)))
+    for r2 in (float("inf"), r2_small):
+        for kind, skips_list in (("bf", (0,)), ("kd", (0, 2)), ("ball", (1, 3))):
+            for skips in skips_list:
+                for heap in (False, True):
+                    plain = oracle.ref_knn(kind, pts, qs, k, r2, skips, heap, fma=False)
+                    fused = oracle.ref_knn(kind, pts, qs, k, r2, skips, heap, fma=True)
+                    for ref_fma, (ri, rd) in ((False, plain), (True, fused)):
+                        # Where the contracted build came out identical to the plain one, the
+                        # host compiler did not fuse it: compare with the plain arithmetic.
+                        fma = ref_fma and not (np.array_equal(ri, plain[0]) and
+                                               np.array_equal(rd.view(np.uint32), plain[1].view(np.uint32)))
+                        if kind == "bf":
+                            oi, od = oracle.bf_knn(pts, qs, k, r2, heap=heap, fma=fma)
+                            assert np.array_equal(oi, ri), (kind, r2, heap, ref_fma)
+                            assert np.array_equal(od.view(np.uint32), rd.view(np.uint32)), (kind, r2, heap, ref_fma)
+                            continue
+                        t = oracle.kd_tree(pts, skips) if kind == "kd" else oracle.ball_tree(pts, skips, fma=fma)
+                        got = t.knn(qs, k, r2, heap=heap, fma=fma, strict=False)
+                        assert np.array_equal(oracle.row_keys(*got), oracle.row_keys(ri, rd)), \
+                            (kind, skips, r2, heap, ref_fma)
