@@ -183,8 +183,9 @@ int k_slot(uint32_t k) {
 }
 
 // Picks the fastest plan for this index and k by timing candidates on up to 32768 of the
-// caller's queries (CUDA events, best of two runs each), in three stages: leaf bucket size,
-// then block size, then tracker/stack storage.  Results are exact for every candidate.
+// caller's queries (8192 for brute force; CUDA events, best of two runs after a warm-up), in
+// three stages: traversal (thread or warp) x leaf bucket size, or the tensor-core filter; then
+// block size; then tracker/stack storage.  Results are exact for every candidate.
 int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t s, knn::QueryPlan* out,
              float* best_ms, uint32_t* tried, bool allow_tc = true) {
     knn::QueryArgs t = a;
