@@ -170,3 +170,51 @@ def test_ctypes_structs_match_the_c_layout(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for field, _ in py._fields_:
             assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
+
+
+def _cuda_device_usable():
+    import torch
+    return torch.cuda.is_available()
+
+
+def test_entry_points_report_a_failing_cuda_runtime():
+    """Where the CUDA runtime fails (here: no device), every entry point that needs it returns
+    KNN_ERR_CUDA with the runtime's message and leaves no handle; nothing throws or crashes, and
+    the stand-in device pointer is never dereferenced."""
+    if _cuda_device_usable():
+        pytest.skip("a CUDA device is present")
+    lib = _lib.load()
+    fake = ctypes.c_void_p(0x1000)
+    calls = {
+        "knn_bf_create": lambda h: lib.knn_bf_create(fake, 100, 3, None, ctypes.byref(h)),
+        "knn_kd_create": lambda h: lib.knn_kd_create(fake, 100, 3, 3, 0, 256, None, ctypes.byref(h)),
+        "knn_ball_create": lambda h: lib.knn_ball_create(fake, 100, 3, 1, 256, None, ctypes.byref(h)),
+        "knn_bf_query_noalloc": lambda h: lib.knn_bf_query_noalloc(fake, 100, 3, fake, 10, 1.0, 4, fake, fake, None),
+        "knn_tc_selftest": lambda h: lib.knn_tc_selftest(16, ctypes.byref(ctypes.c_float()),
+                                                        ctypes.byref(ctypes.c_uint32())),
+    }
+    for name, call in calls.items():
+        h = ctypes.c_void_p(0x1234)
+        assert call(h) == _lib.ERR_CUDA, name
+        assert lib.knn_last_error(), name
+        if name.endswith("_create"):
+            assert not h.value, name
+
+
+def test_dropin_classes_throw_cuda_exception_on_runtime_failure(tmp_path):
+    """The C++ drop-in maps a failing status to KnnTrees::CudaException, as the reference's
+    classes throw it (src/KnnTrees.cuh:20-23)."""
+    if _cuda_device_usable():
+        pytest.skip("a CUDA device is present")
+    exe = tmp_path / "no_device_errors"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    r = subprocess.run(["nvcc", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a",
+                        f"-I{os.path.join(ROOT, 'include')}", os.path.join(ROOT, "tests", "cpp", "no_device_errors.cu"),
+                        "-o", str(exe), f"-L{libdir}", "-lcudaexactknn", f"-Xlinker=-rpath,{libdir}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stdout + out.stderr
+    lines = out.stdout.splitlines()
+    assert [s.split(" ")[0] for s in lines] == ["BruteForceGpu", "KdTreeGpu", "BallTreeGpu"]
+    assert all(" threw: " in s for s in lines)
