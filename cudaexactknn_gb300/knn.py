@@ -51,6 +51,32 @@ def _check_points(points: torch.Tensor, name: str = "points") -> torch.Tensor:
     return points.contiguous()
 
 
+# The C ABI takes raw pointers and trusts the sizes it is given, as the reference's classes do.
+# The checks below hold every size the mirror passes to the sizes of the tensors behind the
+# pointers, so that a wrong shape is an exception here instead of an out-of-bounds access.
+
+def _check_size(points: torch.Tensor, size: int | None) -> int:
+    """Points the index takes: `size` (the reference's size argument) or every row, never more."""
+    rows = int(points.shape[0])
+    n = rows if size is None else int(size)
+    if n < 0 or n > rows:
+        raise ValueError(f"size {n}: points has {rows} rows")
+    return n
+
+
+def _check_dims(t: torch.Tensor, dims: int, name: str) -> None:
+    if t.dim() != 2 or int(t.shape[1]) != dims:
+        raise ValueError(f"{name} must be [count, {dims}] for this index, got {list(t.shape)}")
+
+
+def _check_results(indexes, distances, count: int, k: int, device: torch.device) -> None:
+    """Result buffers the engine writes: contiguous [>= count, k] int32 / float32 on `device`."""
+    for t, dt in ((indexes, torch.int32), (distances, torch.float32)):
+        if (not isinstance(t, torch.Tensor) or t.dtype != dt or t.dim() != 2 or t.shape[0] < count
+                or t.shape[1] != k or not t.is_contiguous() or t.device != device):
+            raise TypeError(f"result buffers must be contiguous [count, k] int32 / float32 tensors on {device}")
+
+
 @dataclass
 class Query:
     """Query<Dims,K> (src/KnnTrees.cuh:224-231): device points and result buffers."""
@@ -106,14 +132,13 @@ class _Index:
 
     def _query(self, query: Query, k: int | None, o: _lib.QueryOpts, sync: bool, stream, radii=None):
         q = _check_points(query.points, "query.points")
+        _check_dims(q, self.dims, "query.points")
         if k is None:
             if query.r_indexes is None:
                 raise ValueError("k is needed when the query has no result buffers")
             k = int(query.r_indexes.shape[1])
         query.ensure_outputs(k)
-        for t, dt in ((query.r_indexes, torch.int32), (query.r_distances, torch.float32)):
-            if t.dtype != dt or t.shape[0] < query.count or t.shape[1] != k or not t.is_contiguous():
-                raise TypeError("result buffers must be contiguous [count, k] int32 / float32")
+        _check_results(query.r_indexes, query.r_distances, query.count, k, q.device)
         if q.shape[0] < query.count:
             raise ValueError("query.points has fewer rows than query.count")
         lib = _lib.load()
@@ -140,8 +165,9 @@ class _Index:
     def batch_knn_radii(self, query: Query, radii: torch.Tensor, k: int | None = None, sync: bool = True,
                         stream=None, **kw):
         """batch_knn with one max_distance2 per query (float32 CUDA tensor [count])."""
-        if radii.dtype != torch.float32 or not radii.is_cuda or radii.numel() < query.count:
-            raise TypeError("radii must be a float32 CUDA tensor with one entry per query")
+        if (radii.dtype != torch.float32 or not radii.is_cuda or radii.numel() < query.count
+                or radii.device != query.points.device):
+            raise TypeError("radii must be a float32 CUDA tensor with one entry per query, on the queries' device")
         o = _lib.opts(**{key: kw[key] for key in kw})
         return self._query(query, k, o, sync, stream, radii=radii.contiguous())
 
@@ -157,11 +183,13 @@ class _Index:
         qt = torch.as_tensor(queries)
         if qt.dtype != torch.float32 or not qt.is_contiguous() or qt.is_cuda:
             raise TypeError("host queries must be a contiguous float32 CPU array")
+        _check_dims(qt, self.dims, "queries")
         count = int(qt.shape[0])
         if out_idx is None:
             out_idx = torch.empty((count, k), dtype=torch.int32, pin_memory=qt.is_pinned())
         if out_dist is None:
             out_dist = torch.empty((count, k), dtype=torch.float32, pin_memory=qt.is_pinned())
+        _check_results(out_idx, out_dist, count, k, torch.device("cpu"))
         o = _lib.opts(block_size, heap, shmem_tracking, shmem_stack, flags, leaf_scan, traversal)
         st = _lib.load().knn_query_host(self._h, qt.data_ptr(), count, float(max_distance2), k,
                                         out_idx.data_ptr(), out_dist.data_ptr(), ctypes.byref(o),
@@ -174,6 +202,7 @@ class _Index:
                            coverage: float = 0.0, seed: int = 0, stream=None) -> _lib.TrainReport:
         """Trains the index's radius model on sample queries (CUDA float32 [count, dims])."""
         s = _check_points(samples, "samples")
+        _check_dims(s, self.dims, "samples")
         o = _lib.TrainOpts()
         o.steps, o.batch, o.lr, o.coverage, o.seed = steps, batch, lr, coverage, seed
         rep = _lib.TrainReport()
@@ -183,6 +212,7 @@ class _Index:
 
     def predict_log_kth(self, queries: torch.Tensor) -> torch.Tensor:
         q = _check_points(queries, "queries")
+        _check_dims(q, self.dims, "queries")
         out = torch.empty(q.shape[0], dtype=torch.float32, device=q.device)
         _lib.check(_lib.load().knn_radius_model_predict(self._h, q.data_ptr(), int(q.shape[0]), out.data_ptr(),
                                                         _stream_handle(None)))
@@ -203,8 +233,12 @@ class _Index:
 
     def stats(self, query: Query, k: int, **kw) -> _lib.QueryCounters:
         """Runs the query with device counters (nodes visited, leaves, points scanned)."""
-        q = _check_points(query.points)
+        q = _check_points(query.points, "query.points")
+        _check_dims(q, self.dims, "query.points")
+        if q.shape[0] < query.count:
+            raise ValueError("query.points has fewer rows than query.count")
         query.ensure_outputs(k)
+        _check_results(query.r_indexes, query.r_distances, query.count, k, q.device)
         o = _lib.opts(**kw)
         out = _lib.QueryCounters()
         st = _lib.load().knn_query_stats(self._h, q.data_ptr(), query.count, float(query.max_distance2), k,
@@ -222,7 +256,7 @@ class BruteForceGpu(_Index):
     def __init__(self, points: torch.Tensor, size: int | None = None, stream=None):
         super().__init__()
         p = _check_points(points)
-        n = int(p.shape[0] if size is None else size)
+        n = _check_size(p, size)
         self.dims = int(p.shape[1])
         _lib.check(_lib.load().knn_bf_create(p.data_ptr(), n, self.dims, _stream_handle(stream),
                                              ctypes.byref(self._h)))
@@ -237,7 +271,7 @@ class KdTreeGpu(_Index):
                  aux_dims: int | None = None, c_block_size: int = 256, stream=None):
         super().__init__()
         p = _check_points(points)
-        n = int(p.shape[0] if size is None else size)
+        n = _check_size(p, size)
         self.dims = int(p.shape[1])
         aux = self.dims if aux_dims is None else int(aux_dims)
         _lib.check(_lib.load().knn_kd_create(p.data_ptr(), n, self.dims, aux, depth_skips, c_block_size,
@@ -253,7 +287,7 @@ class BallTreeGpu(_Index):
                  c_block_size: int = 256, stream=None):
         super().__init__()
         p = _check_points(points)
-        n = int(p.shape[0] if size is None else size)
+        n = _check_size(p, size)
         self.dims = int(p.shape[1])
         _lib.check(_lib.load().knn_ball_create(p.data_ptr(), n, self.dims, depth_skips, c_block_size,
                                                _stream_handle(stream), ctypes.byref(self._h)))
