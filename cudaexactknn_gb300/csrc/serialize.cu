@@ -55,6 +55,9 @@ struct Shape {
 
 int derive_shape(uint32_t structure, uint32_t n, uint32_t dims, uint32_t aux_dims, uint32_t skips, Shape* sh) {
     if (dims < 1 || dims > knn::kMaxDims) return knn::fail(KNN_ERR_INVALID_ARGUMENT, "serialised index: dims %u", dims);
+    // Construction accepts n < 2^31 only; beyond it the tree shape arithmetic below would shift
+    // a 32-bit value by 32.
+    if (n > 0x7FFFFFFFu) return knn::fail(KNN_ERR_INVALID_ARGUMENT, "serialised index: n %u >= 2^31", n);
     if (structure != KNN_BRUTE_FORCE && structure != KNN_KD_TREE && structure != KNN_BALL_TREE)
         return knn::fail(KNN_ERR_INVALID_ARGUMENT, "serialised index: structure %u", structure);
     if (aux_dims < 1 || aux_dims > dims || (structure != KNN_KD_TREE && aux_dims != dims))

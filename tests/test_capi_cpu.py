@@ -92,7 +92,8 @@ def _blob(structure=1, n=1000, dims=3, aux=3, skips=0, has_model=0, model_k=0, s
     return head + payload
 
 
-@pytest.mark.parametrize("case", ["short", "magic", "version", "sizes", "total", "checksum", "skips", "aux", "model"])
+@pytest.mark.parametrize("case", ["short", "magic", "version", "sizes", "total", "checksum", "skips", "aux", "model",
+                                  "n"])
 def test_deserialize_rejects_malformed_blobs_without_a_device(case):
     """knn_index_deserialize validates the header, the array sizes the shape implies, the total
     size and the checksum before it touches the device (a kd tree of n=1000, dims 3, skips 0:
@@ -119,13 +120,18 @@ def test_deserialize_rejects_malformed_blobs_without_a_device(case):
         blob = _blob(**dict(kw, skips=12))
     elif case == "aux":
         blob = _blob(**dict(kw, aux=4))
-    else:
+    elif case == "model":
         blob = _blob(**dict(kw, has_model=1, model_k=16))
+    else:
+        # n beyond construction's limit (2^31 - 1), sizes as a kd tree of 2^32 leaves would have.
+        blob = _blob(**dict(kw, n=0xFFFFFFFF, sizes=(0, 4 * (2 ** 32 - 1), 16 * 2 ** 32, 0, 0)))
     h = ctypes.c_void_p()
     buf = ctypes.create_string_buffer(blob, len(blob))
     assert lib.knn_index_deserialize(buf, len(blob), None, ctypes.byref(h)) == _lib.ERR_INVALID_ARGUMENT
     assert not h.value
     assert b"serialised index" in lib.knn_last_error()
+    if case == "n":
+        assert b"2^31" in lib.knn_last_error()
 
 
 def _header_prototypes():
