@@ -17,6 +17,8 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
+#include <new>
 #include <tuple>
 #include <vector>
 
@@ -148,14 +150,14 @@ int check_item(const knn_batch_item& it) {
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-int knn_batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, void* stream, knn_batch** out) {
+int batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, void* stream, knn_batch** out) {
     if (!out || (count && !items)) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
     *out = nullptr;
     for (uint32_t i = 0; i < count; ++i) KNN_TRY(check_item(items[i]));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    auto* b = new knn_batch();
+    std::unique_ptr<knn_batch> b(new knn_batch());
     b->items.assign(items, items + count);
     std::map<std::tuple<int, uint32_t, uint32_t>, uint32_t> class_of;
     for (uint32_t i = 0; i < count; ++i) {
@@ -326,12 +328,23 @@ int knn_batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags
             }
         }
     }
-    if (rc != KNN_OK) {
-        delete b;
-        return rc;
-    }
-    *out = b;
+    if (rc != KNN_OK) return rc;
+    *out = b.release();
     return KNN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// The plan's containers allocate host memory; an allocation failure there is a status, not an
+// exception thrown across the C ABI.
+int knn_batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, void* stream, knn_batch** out) {
+    try {
+        return batch_create(items, count, flags, stream, out);
+    } catch (const std::bad_alloc&) {
+        return fail(KNN_ERR_OUT_OF_MEMORY, "host allocation failed while planning the batch");
+    }
 }
 
 int knn_batch_run(knn_batch* batch, void* stream) {

@@ -224,3 +224,17 @@ def test_dropin_classes_throw_cuda_exception_on_runtime_failure(tmp_path):
     lines = out.stdout.splitlines()
     assert [s.split(" ")[0] for s in lines] == ["BruteForceGpu", "KdTreeGpu", "BallTreeGpu"]
     assert all(" threw: " in s for s in lines)
+
+
+def test_empty_batch_needs_no_device():
+    """A batch with no items plans, runs, reports and frees without touching the device."""
+    lib = _lib.load()
+    b = ctypes.c_void_p()
+    assert lib.knn_batch_create(None, 0, 0, None, ctypes.byref(b)) == _lib.OK and b.value
+    classes, kernels = ctypes.c_uint32(7), ctypes.c_uint32(7)
+    assert lib.knn_batch_info(b, ctypes.byref(classes), ctypes.byref(kernels)) == _lib.OK
+    assert (classes.value, kernels.value) == (0, 0)
+    assert lib.knn_batch_run(b, None) == _lib.OK
+    assert lib.knn_batch_destroy(b) == _lib.OK
+    assert lib.knn_batch_create(None, 2, 0, None, ctypes.byref(b)) == _lib.ERR_INVALID_ARGUMENT
+    assert not b.value
