@@ -153,8 +153,8 @@ int check_item(const knn_batch_item& it) {
 namespace {
 
 int batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, void* stream, knn_batch** out) {
+    if (out) *out = nullptr;
     if (!out || (count && !items)) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
-    *out = nullptr;
     for (uint32_t i = 0; i < count; ++i) KNN_TRY(check_item(items[i]));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     std::unique_ptr<knn_batch> b(new knn_batch());

@@ -142,8 +142,8 @@ int knn_index_serialize(const knn_index* index, void* host_buf, size_t capacity,
 }
 
 int knn_index_deserialize(const void* host_buf, size_t size, void* stream, knn_index** out) {
+    if (out) *out = nullptr;
     if (!host_buf || !out) return knn::fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
-    *out = nullptr;
     if (size < sizeof(Header)) return knn::fail(KNN_ERR_INVALID_ARGUMENT, "serialised index: %zu bytes", size);
     Header h;
     std::memcpy(&h, host_buf, sizeof(Header));

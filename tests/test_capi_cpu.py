@@ -132,6 +132,10 @@ def test_deserialize_rejects_malformed_blobs_without_a_device(case):
     assert b"serialised index" in lib.knn_last_error()
     if case == "n":
         assert b"2^31" in lib.knn_last_error()
+    # A missing blob is refused too, and the handle is cleared.
+    h = ctypes.c_void_p(0x1234)
+    assert lib.knn_index_deserialize(None, len(blob), None, ctypes.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    assert not h.value
 
 
 def _header_prototypes():
