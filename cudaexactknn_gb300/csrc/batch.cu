@@ -340,11 +340,7 @@ extern "C" {
 // The plan's containers allocate host memory; an allocation failure there is a status, not an
 // exception thrown across the C ABI.
 int knn_batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, void* stream, knn_batch** out) {
-    try {
-        return batch_create(items, count, flags, stream, out);
-    } catch (const std::bad_alloc&) {
-        return fail(KNN_ERR_OUT_OF_MEMORY, "host allocation failed while planning the batch");
-    }
+    return knn::no_throw([&] { return batch_create(items, count, flags, stream, out); });
 }
 
 int knn_batch_run(knn_batch* batch, void* stream) {

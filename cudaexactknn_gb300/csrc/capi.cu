@@ -75,7 +75,7 @@ int create_common(knn_index* ix, cudaStream_t s, BuildFn&& build) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    int rc = ix->n ? build() : KNN_OK;
+    int rc = ix->n ? knn::no_throw(build) : KNN_OK;
     if (rc == KNN_OK) {
         cudaEventRecord(e1, s);
         const cudaError_t e = cudaEventSynchronize(e1);
@@ -309,7 +309,7 @@ int tune_plan(knn_index* ix, const QueryArgs& a, cudaStream_t s, QueryPlan* out)
 
 namespace {
 
-int run_query(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts, cudaStream_t s) {
+int run_query_checked(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts, cudaStream_t s) {
     if (!ix) return fail(KNN_ERR_INVALID_ARGUMENT, "index is null");
     if (a.k == 0) return fail(KNN_ERR_INVALID_ARGUMENT, "k must be >= 1");
     if (a.k > knn::kMaxK) return fail(KNN_ERR_UNSUPPORTED, "k %u > %u", a.k, knn::kMaxK);
@@ -350,6 +350,12 @@ int run_query(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts
     }
     if (flags & KNN_QF_SYNC) KNN_TRY_CUDA(cudaStreamSynchronize(s));
     return KNN_OK;
+}
+
+// Every query entry point: the tensor-core filter builds its layout on first use with host
+// containers, the autotuner keeps plans in the index.
+int run_query(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts, cudaStream_t s) {
+    return knn::no_throw([&] { return run_query_checked(ix, a, opts, s); });
 }
 
 }  // namespace
@@ -525,7 +531,7 @@ int knn_tuned_plan(const knn_index* index, uint32_t k, uint32_t learned_radius, 
 int knn_tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* mismatches) {
     if (!max_rel_err || !mismatches) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
     if (dims == 0 || dims > 128) return fail(KNN_ERR_UNSUPPORTED, "dims %u", dims);
-    return knn::tc_selftest(dims, max_rel_err, mismatches);
+    return knn::no_throw([&] { return knn::tc_selftest(dims, max_rel_err, mismatches); });
 }
 
 uint64_t knn_launch_count(void) { return knn::g_launches.load(); }
@@ -543,7 +549,7 @@ int knn_radius_model_train(knn_index* index, const float* d_samples, uint32_t co
     if (!(o.lr > 0.0f)) o.lr = 3e-3f;
     if (!(o.coverage > 0.0f && o.coverage < 1.0f)) o.coverage = 0.98f;
     if (!o.seed) o.seed = 1;
-    return knn::model_train(index, d_samples, count, k, o, as_stream(stream), report);
+    return knn::no_throw([&] { return knn::model_train(index, d_samples, count, k, o, as_stream(stream), report); });
 }
 
 int knn_radius_model_predict(knn_index* index, const float* d_queries, uint32_t count, float* d_log_kth,
@@ -600,12 +606,14 @@ int knn_radius_model_gradients(const float* h_params, uint32_t dims, const float
     KNN_TRY(knn::model_gradients(prm, dims, x, t, nullptr, batch, grad, loss, scratch, nullptr));
     const size_t trainable = np - dims * 32 - 2 * dims - 1;  // fixed projection, scaling, margin follow
     KNN_TRY_CUDA(cudaMemcpy(h_grad, grad, trainable * 4, cudaMemcpyDeviceToHost));
-    std::vector<float> lr(batch);
-    KNN_TRY_CUDA(cudaMemcpy(lr.data(), loss, static_cast<size_t>(batch) * 4, cudaMemcpyDeviceToHost));
-    double total = 0;
-    for (float v : lr) total += v;
-    *h_loss = static_cast<float>(total);
-    return KNN_OK;
+    return knn::no_throw([&]() -> int {
+        std::vector<float> lr(batch);
+        KNN_TRY_CUDA(cudaMemcpy(lr.data(), loss, static_cast<size_t>(batch) * 4, cudaMemcpyDeviceToHost));
+        double total = 0;
+        for (float v : lr) total += v;
+        *h_loss = static_cast<float>(total);
+        return KNN_OK;
+    });
 }
 
 const char* knn_status_string(int status) {

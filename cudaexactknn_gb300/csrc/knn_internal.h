@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdint>
 #include <initializer_list>
+#include <new>
 #include <vector>
 
 #include "../../include/cudaexactknn.h"
@@ -38,6 +39,19 @@ void note_launches(uint32_t n);
         int knn_rc_ = (expr);           \
         if (knn_rc_ != KNN_OK) return knn_rc_; \
     } while (0)
+
+// Runs f() and turns an exception from host code (a container's std::bad_alloc) into a status,
+// so that nothing thrown crosses the C ABI.
+template <class F>
+int no_throw(F&& f) noexcept {
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return fail(KNN_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (...) {
+        return fail(KNN_ERR_CUDA, "unexpected exception in host code");
+    }
+}
 
 // ---- dimension padding ------------------------------------------------------------------------
 // Kernels are compiled for padded dimension counts; padded coordinates are zero in both points
