@@ -242,3 +242,10 @@ def test_empty_batch_needs_no_device():
     assert lib.knn_batch_destroy(b) == _lib.OK
     assert lib.knn_batch_create(None, 2, 0, None, ctypes.byref(b)) == _lib.ERR_INVALID_ARGUMENT
     assert not b.value
+
+
+def test_library_is_not_older_than_its_sources():
+    """The tests run the library as built: a source edited after the last build (or a build that
+    failed and left the previous library in place) would make them test stale code."""
+    from cudaexactknn_gb300 import build
+    assert os.path.getmtime(_lib.LIB_PATH) >= build._deps_mtime(), "rebuild: python -c 'import __graft_entry__ as g; g.build()'"
