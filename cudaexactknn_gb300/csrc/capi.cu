@@ -542,6 +542,8 @@ int knn_radius_model_train(knn_index* index, const float* d_samples, uint32_t co
     if (index->n == 0) return fail(KNN_ERR_INVALID_ARGUMENT, "empty point set");
     if (count < 16) return fail(KNN_ERR_INVALID_ARGUMENT, "need at least 16 samples (got %u)", count);
     if (k == 0 || k > knn::kMaxK) return fail(k ? KNN_ERR_UNSUPPORTED : KNN_ERR_INVALID_ARGUMENT, "k %u", k);
+    // With fewer than k points every sample's k-th distance is unbounded: no target to learn.
+    if (k > index->n) return fail(KNN_ERR_INVALID_ARGUMENT, "k %u exceeds the %u points of the index", k, index->n);
     knn_train_opts o{};
     if (opts) o = *opts;
     if (!o.steps) o.steps = 3000;

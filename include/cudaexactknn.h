@@ -220,7 +220,8 @@ KNN_API int knn_batch_destroy(knn_batch* batch);
  *      src/KnnTrees.cuh:228, per query) ---------------------------------------------------------
  * Trains the index's D->64->64->1 radius model on `count` sample queries (device float32
  * [count][dims]): exact k-th distances from the engine's own search are the targets; forward,
- * backward and Adam run on the GPU; the margin is calibrated to `coverage`.  Synchronous. */
+ * backward and Adam run on the GPU; the margin is calibrated to `coverage`.  Synchronous.
+ * k must not exceed the index's point count (every k-th distance would be unbounded). */
 KNN_API int knn_radius_model_train(knn_index* index, const float* d_samples, uint32_t count, uint32_t k,
                                    const knn_train_opts* opts, void* stream, knn_train_report* report);
 /* Predicted natural log of the k-th squared distance per query (device float32 [count]). */
