@@ -153,6 +153,7 @@ int check_item(const knn_batch_item& it) {
 namespace {
 
 int batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, void* stream, knn_batch** out) {
+    const knn::Range range("knn batch create");
     if (out) *out = nullptr;
     if (!out || (count && !items)) return fail(KNN_ERR_INVALID_ARGUMENT, "null argument");
     for (uint32_t i = 0; i < count; ++i) KNN_TRY(check_item(items[i]));
@@ -346,6 +347,7 @@ int knn_batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags
 int knn_batch_run(knn_batch* batch, void* stream) {
     if (!batch) return fail(KNN_ERR_INVALID_ARGUMENT, "batch is null");
     if (!batch->exec) return KNN_OK;  // nothing to run (every item had zero queries)
+    const knn::Range range("knn batch run");
     KNN_TRY_CUDA(cudaGraphLaunch(batch->exec, static_cast<cudaStream_t>(stream)));
     knn::note_launches(1);
     return KNN_OK;

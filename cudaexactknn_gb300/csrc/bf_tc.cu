@@ -1907,6 +1907,7 @@ bool tc_supported(uint32_t dims, uint32_t k) {
 int tc_prepare(knn_index* ix, cudaStream_t s) {
     auto& T = ix->tc;
     if (T.ready) return T.usable ? KNN_OK : fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: coordinates out of range");
+    const Range range("tensor-core filter layout");
     const uint32_t n = ix->n, dims = ix->dims, ps = round_up4(ix->dp), H = halves(dims);
     // Dense source rows: the brute-force points, or a tree's occupied leaf slots in slot order.
     DevBuf dense_buf;
@@ -2351,6 +2352,7 @@ static int rescore(RescoreArgs ra, uint32_t count, cudaStream_t s) {
 uint32_t tc_default_cap(uint32_t k) { return std::min(4096u, std::max(1024u, 16u * k)); }
 
 int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaStream_t s) {
+    const Range range("tensor-core filter query");
     const uint32_t H = halves(ix->dims);
     if (!tc_supported(ix->dims, a.k)) return fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: dims %u, k %u", ix->dims, a.k);
     QueryPlan plain = plan;

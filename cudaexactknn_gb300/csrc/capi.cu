@@ -70,6 +70,7 @@ void tree_shape(knn_index* ix, uint32_t skips, bool ball) {
 
 template <class BuildFn>
 int create_common(knn_index* ix, cudaStream_t s, BuildFn&& build) {
+    const knn::Range range("knn create");
     cudaGetDevice(&ix->device);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
@@ -139,6 +140,7 @@ int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& p
     // The tensor-core filter tightens each query's bound from its own cell's points before it
     // skips tiles; a seed would only add retries, so it runs unseeded.
     if (plan.bf16) return dispatch(ix, a, plan, s);
+    const knn::Range range("learned-radius search");
     const size_t n = a.count;
     const uint32_t* order = nullptr;
     if (plan.reorder && a.count >= 4096) {
@@ -188,6 +190,7 @@ int k_slot(uint32_t k) {
 // block size; then tracker/stack storage.  Results are exact for every candidate.
 int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t s, knn::QueryPlan* out,
              float* best_ms, uint32_t* tried, bool allow_tc = true) {
+    const knn::Range range("autotune");
     knn::QueryArgs t = a;
     // Brute force costs n distances per query; a smaller sample keeps tuning short.
     t.count = std::min<uint32_t>(a.count, ix->structure == KNN_BRUTE_FORCE ? 8192u : 32768u);
@@ -355,6 +358,7 @@ int run_query_checked(knn_index* ix, const knn::QueryArgs& a, const knn_query_op
 // Every query entry point: the tensor-core filter builds its layout on first use with host
 // containers, the autotuner keeps plans in the index.
 int run_query(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts, cudaStream_t s) {
+    const knn::Range range("knn query");
     return knn::no_throw([&] { return run_query_checked(ix, a, opts, s); });
 }
 
@@ -551,6 +555,7 @@ int knn_radius_model_train(knn_index* index, const float* d_samples, uint32_t co
     if (!(o.lr > 0.0f)) o.lr = 3e-3f;
     if (!(o.coverage > 0.0f && o.coverage < 1.0f)) o.coverage = 0.98f;
     if (!o.seed) o.seed = 1;
+    const knn::Range range("radius model training");
     return knn::no_throw([&] { return knn::model_train(index, d_samples, count, k, o, as_stream(stream), report); });
 }
 

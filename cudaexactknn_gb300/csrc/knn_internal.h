@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdarg>
 #include <cstdint>
@@ -39,6 +40,15 @@ void note_launches(uint32_t n);
         int knn_rc_ = (expr);           \
         if (knn_rc_ != KNN_OK) return knn_rc_; \
     } while (0)
+
+// Names a host-side phase (construction, a query, the autotuner, training, a batch) for
+// profilers as an NVTX range; without a profiler attached a push/pop pair is a pointer check.
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
 
 // Runs f() and turns an exception from host code (a container's std::bad_alloc) into a status,
 // so that nothing thrown crosses the C ABI.
