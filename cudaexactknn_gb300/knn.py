@@ -263,7 +263,7 @@ class BruteForceGpu(_Index):
 
 
 class KdTreeGpu(_Index):
-    """KdTreeGpu<Dims,AuxDims,CBlockSize> (src/KdTreeGpu.cuh:444-574)."""
+    """KdTreeGpu<Dims,AuxDims,CBlockSize> (src/KdTreeGpu.cuh:282-412: constructor 375-385, batchKnn 393-410)."""
 
     structure = _lib.KD_TREE
 

@@ -1,6 +1,7 @@
 // KdTreeGpu.cuh -- drop-in replacement of src/KdTreeGpu.cuh (rezvoj/CudaExactKnn) on the GB300
 // engine.  Same class template (AuxDims defaults to Dims, CBlockSize to 256), constructor with
-// depthSkips, and batchKnn<K, BLOCK_SIZE, HEAP, SH_NN, SH_STACK> (src/KdTreeGpu.cuh:444-574).
+// depthSkips, and batchKnn<K, BLOCK_SIZE, HEAP, SH_NN, SH_STACK> (src/KdTreeGpu.cuh:282-412; constructor
+// 375-385, batchKnn 393-410).
 #pragma once
 
 // Standard headers the reference's version brings in (directly or through <cub/cub.cuh>);
