@@ -32,6 +32,7 @@ QF_LEARNED_RADIUS = 4
 QF_BF16_FILTER = 8
 QF_KEEP_ORDER = 16
 QF_TIMING = 32
+QF_TEST_FILTER_GIVE_UP = 0x40000000
 
 
 class QueryOpts(ctypes.Structure):
@@ -44,7 +45,7 @@ class QueryOpts(ctypes.Structure):
 class QueryCounters(ctypes.Structure):
     _fields_ = [("nodes_visited", ctypes.c_uint64), ("leaves_visited", ctypes.c_uint64),
                 ("points_scanned", ctypes.c_uint64), ("fallback_queries", ctypes.c_uint64),
-                ("reserved", ctypes.c_uint64 * 4)]
+                ("filter_give_ups", ctypes.c_uint64), ("reserved", ctypes.c_uint64 * 3)]
 
 
 class IndexInfo(ctypes.Structure):

@@ -281,10 +281,10 @@ static int launch_ball(knn_index* ix, const QueryArgs& a, const QueryPlan& plan,
     p.out_idx = a.out_idx;
     p.out_dist = a.out_dist;
     p.counters = a.counters;
-    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));
+    if (plan.timing) KNN_TRY(ix->timing.begin(s));
     kern<<<ceil_div(a.count, block), block, smem, s>>>(p);
     KNN_LAUNCHED();
-    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
+    if (plan.timing) KNN_TRY(ix->timing.end(s));
     return KNN_OK;
 }
 

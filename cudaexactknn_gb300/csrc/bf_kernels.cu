@@ -62,10 +62,10 @@ static int launch_bf(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, c
         p.partial = ix->workspace.as<uint64_t>();
     }
     dim3 grid(qblocks, splits);
-    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));
+    if (plan.timing) KNN_TRY(ix->timing.begin(s));
     kern<<<grid, block, smem, s>>>(p);
     KNN_LAUNCHED();
-    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
+    if (plan.timing) KNN_TRY(ix->timing.end(s));
     if (splits > 1) {
         bf_merge_kernel<KMAX><<<ceil_div(a.count, 128), 128, 0, s>>>(p.partial, splits, a.count, a.k, a.max_d2,
                                                                       a.radii, a.order, a.count_dev, a.out_idx,

@@ -16,6 +16,9 @@
 //     because the merge kernel reads only slots the search kernel wrote earlier in the same call;
 //   * the first call on each device looks up the array's device address (cudaGetSymbolAddress,
 //     with that device current) and caches it; make that first call before any stream capture.
+//     The cached address belongs to the device's primary context: after a cudaDeviceReset of
+//     that device (which also invalidates every index of this library on it) it is stale, so do
+//     not call this entry point again in a process that has reset the device.
 
 #include <algorithm>
 #include <mutex>

@@ -145,6 +145,7 @@ struct TcParams {
     float* final_t;              // [nq] the row's k-th upper bound T' after the last tile
     DevCounters* counters;
     int* error;
+    uint32_t give_up;            // tests: the producer gives up after its first point-tile copy
 };
 
 // Heap of a thread's k smallest upper bounds (max at slot 0), slot-major in shared memory.
@@ -362,7 +363,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 for (uint32_t st = 0; ok && st < 3; ++st) {
                     if (st == 2) ok = marker(kBoundary, 0) && mbar_wait(mask_ready, tiles & 1, abort) && !*abort;
                     seq.begin(st);
-                    while (ok && seq.next(&item, &centre)) ok = load(item, centre);
+                    while (ok && seq.next(&item, &centre)) {
+                        ok = load(item, centre);
+                        if (p.give_up) ok = false;  // tests: as if the next wait had run out
+                    }
                 }
                 uint32_t next = kNone;
                 if (ok) {
@@ -748,7 +752,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     }
     tc_fence_before();
     __syncthreads();
-    if (*abort && threadIdx.x == 0) atomicExch(p.error, 1);
+    if (*abort && threadIdx.x == 0) {
+        atomicExch(p.error, 1);
+        if (p.counters) atomicAdd(&p.counters->give_ups, 1);
+    }
     if (warp == 1) {
         tc_fence_after();
         tmem_dealloc(tmem, kCols);
@@ -2462,6 +2469,7 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     p.final_t = final_t;
     p.counters = a.counters;
     p.error = reinterpret_cast<int*>(small + 1);
+    p.give_up = plan.test_give_up ? 1u : 0u;
     p.qtiles = qtiles;
     p.tile_counter = small + 2;
     // Rows no block settles (a block that gave up) keep these: the plain search within a huge radius.
@@ -2481,10 +2489,10 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     if ((H >= 32) != T.tree || (H == 32 && T.bd != 16) || (H == 64 && T.bd != 32))
         return fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: layout %u for a %s layout", H, T.tree ? "tree" : "landmark");
     KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));
+    if (plan.timing) KNN_TRY(ix->timing.begin(s));
     kern<<<grid, kThreads, smem, s>>>(p);
     KNN_LAUNCHED();
-    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
+    if (plan.timing) KNN_TRY(ix->timing.end(s));
 
     RescoreArgs ra{};
     ra.pts = T.pts.as<float>();

@@ -113,10 +113,12 @@ int make_plan(const knn_index* ix, const knn_query_opts* o, knn::QueryPlan* p) {
     p->reorder = (o->flags & KNN_QF_KEEP_ORDER) == 0;
     p->timing = (o->flags & KNN_QF_TIMING) != 0;
     p->bf16 = (o->flags & KNN_QF_BF16_FILTER) != 0;
+    p->test_give_up = (o->flags & KNN_QF_TEST_FILTER_GIVE_UP) != 0;
     p->tc_cap = o->reserved;
     p->leaf_scan = o->leaf_scan;
-    if (o->traversal > 1) return fail(KNN_ERR_INVALID_ARGUMENT, "traversal %u: 0 or 1", o->traversal);
+    if (o->traversal > 2) return fail(KNN_ERR_INVALID_ARGUMENT, "traversal %u: 0, 1 or 2", o->traversal);
     p->warp = o->traversal == 1;
+    p->group = o->traversal == 2 && ix->structure == KNN_KD_TREE;
     (void)ix;
     return KNN_OK;
 }
@@ -155,12 +157,13 @@ int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& p
     void* scratch = c.take<uint8_t>(knn::retry_scratch_bytes(a.count));
     KNN_TRY(knn::model_predict(ix->model.as<float>(), ix->dims, a.queries, a.count, a.max_d2, a.radii, radii,
                                nullptr, s, true));
+    // The warp-group k-d search settles or hands on every query itself (no retry rounds).
+    if (plan.group && ix->structure == KNN_KD_TREE)
+        return knn::kd_group_query(ix, a, plan, order, radii, list, list_count, s);
     knn::QueryArgs seeded = a;
     seeded.radii = radii;
     seeded.order = order;
     KNN_TRY(dispatch(ix, seeded, plan, s));
-    knn::QueryPlan again_plan = plan;
-    again_plan.timing = false;  // the timed kernel span stays the seeded search
     for (int round = 0; round < kSeedRounds; ++round) {
         const float grow = round + 1 < kSeedRounds ? kSeedGrowth : INFINITY;
         KNN_TRY(knn::model_retry_list(order, a.out_idx, a.count, a.k, radii, a.max_d2, a.radii, grow, list,
@@ -169,7 +172,7 @@ int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& p
         again.radii = radii;
         again.order = list;
         again.count_dev = list_count;
-        KNN_TRY(dispatch(ix, again, again_plan, s));
+        KNN_TRY(dispatch(ix, again, plan, s));
     }
     return KNN_OK;
 }
@@ -232,12 +235,24 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
     do {
         // The tensor-core filter, for dims >= 16 (the form it is built for), on any structure.
         const bool try_tc = allow_tc && ix->dims >= 16 && knn::tc_supported(ix->dims, a.k);
+        if (ix->structure == KNN_KD_TREE && ix->dp <= 16 && a.k <= 32) {
+            // The warp-group search, seeded by the radius model or by each query's own subtree.
+            for (uint32_t leaf : {4u, 8u, 16u, 32u}) {
+                knn::QueryPlan p;
+                p.block = 128;
+                p.group = true;
+                p.leaf_scan = leaf;
+                if ((rc = consider(p)) != KNN_OK) break;
+            }
+            if (rc != KNN_OK) break;
+        }
         if (ix->structure != KNN_BRUTE_FORCE) {
             for (bool warp : {false, true}) {
                 for (uint32_t leaf : {0u, 4u, 8u, 16u, 32u, 64u}) {
                     if (leaf && leaf <= ix->leaf_slots) continue;
                     knn::QueryPlan p = best;
                     p.bf16 = false;
+                    p.group = false;
                     p.warp = warp;
                     p.leaf_scan = leaf;
                     if ((rc = consider(p)) != KNN_OK) break;
@@ -261,14 +276,14 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
         }
         const knn::QueryPlan stage2 = best;
         for (uint32_t block : {32u, 64u, 256u}) {
-            if (stage2.bf16) break;  // the filter kernel has a fixed shape
+            if (stage2.bf16 || stage2.group) break;  // the filter and group kernels have fixed shapes
             knn::QueryPlan p = stage2;
             p.block = block;
             if ((rc = consider(p)) != KNN_OK) break;
         }
         if (rc != KNN_OK) break;
         const knn::QueryPlan stage3 = best;
-        for (int v = 1; v < 8 && !stage3.bf16; ++v) {
+        for (int v = 1; v < 8 && !stage3.bf16 && !stage3.group; ++v) {
             knn::QueryPlan p = stage3;
             p.heap = v & 1;
             p.sh_nn = (v >> 1) & 1;
@@ -333,17 +348,17 @@ int run_query_checked(knn_index* ix, const knn::QueryArgs& a, const knn_query_op
             KNN_TRY(autotune(ix, a, learned, s, &slot.plan, &slot.ms, &slot.candidates));
             slot.valid = true;
         }
-        const bool timing = plan.timing;
+        const bool timing = plan.timing, give_up = plan.test_give_up;
         plan = slot.plan;
         plan.timing = timing;
+        plan.test_give_up = give_up;
         plan.reorder = plan.reorder && (flags & KNN_QF_KEEP_ORDER) == 0;
     }
     if (plan.timing) {
         KNN_TRY(ix->timing.ensure());
         ix->timing.valid = false;
+        ix->timing.spans = 0;
         KNN_TRY_CUDA(cudaEventRecord(ix->timing.total0, s));
-        KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));  // empty kernel span if none runs
-        KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
     }
     const int rc = learned && ix->n > 0 ? seeded_query(ix, a, plan, s) : dispatch(ix, a, plan, s);
     if (rc != KNN_OK) return rc;
@@ -359,7 +374,11 @@ int run_query_checked(knn_index* ix, const knn::QueryArgs& a, const knn_query_op
 // containers, the autotuner keeps plans in the index.
 int run_query(knn_index* ix, const knn::QueryArgs& a, const knn_query_opts* opts, cudaStream_t s) {
     const knn::Range range("knn query");
-    return knn::no_throw([&] { return run_query_checked(ix, a, opts, s); });
+    return knn::no_throw([&] {
+        if (ix) KNN_TRY(ix->order_guard.before(s));
+        KNN_TRY(run_query_checked(ix, a, opts, s));
+        return ix ? ix->order_guard.after(s) : KNN_OK;
+    });
 }
 
 }  // namespace
@@ -468,20 +487,63 @@ int knn_query_host(knn_index* index, const float* h_queries, uint32_t count, flo
     if (!h_queries || !h_indexes || !h_distances) return fail(KNN_ERR_INVALID_ARGUMENT, "null host pointer");
     if (k == 0 || k > knn::kMaxK) return fail(k == 0 ? KNN_ERR_INVALID_ARGUMENT : KNN_ERR_UNSUPPORTED, "k %u", k);
     cudaStream_t s = as_stream(stream);
-    const size_t qb = static_cast<size_t>(count) * index->dims * sizeof(float);
-    const size_t rb = static_cast<size_t>(count) * k * sizeof(int32_t);
+    const size_t qrow = static_cast<size_t>(index->dims) * sizeof(float);
+    const size_t rrow = static_cast<size_t>(k) * sizeof(int32_t);
+    const size_t qb = count * qrow, rb = count * rrow;
     KNN_TRY(index->staging.reserve(knn::carve_bytes({qb, rb, rb})));
     knn::Carver c(index->staging.ptr);
     float* dq = c.take<float>(static_cast<size_t>(count) * index->dims);
     int32_t* di = c.take<int32_t>(static_cast<size_t>(count) * k);
     float* dd = c.take<float>(static_cast<size_t>(count) * k);
-    KNN_TRY_CUDA(cudaMemcpyAsync(dq, h_queries, qb, cudaMemcpyHostToDevice, s));
-    knn::QueryArgs a{dq, count, max_distance2, nullptr, k, di, dd, nullptr};
-    KNN_TRY(run_query(index, a, opts, s));
-    KNN_TRY_CUDA(cudaMemcpyAsync(h_indexes, di, rb, cudaMemcpyDeviceToHost, s));
-    KNN_TRY_CUDA(cudaMemcpyAsync(h_distances, dd, rb, cudaMemcpyDeviceToHost, s));
+    // Chunks of at least 131,072 queries (smaller ones would leave the GPU part idle), at most 8.
+    constexpr uint32_t kMinChunk = 131072;
+    const uint32_t chunks = std::min<uint32_t>(knn::HostIo::kMaxChunks, std::max(1u, count / kMinChunk));
+    if (chunks == 1) {
+        KNN_TRY_CUDA(cudaMemcpyAsync(dq, h_queries, qb, cudaMemcpyHostToDevice, s));
+        knn::QueryArgs a{dq, count, max_distance2, nullptr, k, di, dd, nullptr};
+        KNN_TRY(run_query(index, a, opts, s));
+        KNN_TRY_CUDA(cudaMemcpyAsync(h_indexes, di, rb, cudaMemcpyDeviceToHost, s));
+        KNN_TRY_CUDA(cudaMemcpyAsync(h_distances, dd, rb, cudaMemcpyDeviceToHost, s));
+        KNN_TRY_CUDA(cudaStreamSynchronize(s));
+        return KNN_OK;
+    }
+    // Copy-in, search and copy-out overlap across chunks: the copy streams start after the work
+    // already queued on the caller's stream (which may still read the staging buffers), chunk i's
+    // search waits for its copy-in, its copy-out for its search, and the caller's stream ends
+    // after the last copy-out.
+    knn::HostIo& io = index->host_io;
+    KNN_TRY(io.ensure());
+    KNN_TRY_CUDA(cudaEventRecord(io.start, s));
+    KNN_TRY_CUDA(cudaStreamWaitEvent(io.in, io.start, 0));
+    KNN_TRY_CUDA(cudaStreamWaitEvent(io.out, io.start, 0));
+    const uint32_t per = (count + chunks - 1) / chunks;
+    for (uint32_t i = 0; i < chunks; ++i) {
+        const size_t first = static_cast<size_t>(i) * per, n = std::min<size_t>(per, count - first);
+        KNN_TRY_CUDA(cudaMemcpyAsync(dq + first * index->dims, h_queries + first * index->dims, n * qrow,
+                                     cudaMemcpyHostToDevice, io.in));
+        KNN_TRY_CUDA(cudaEventRecord(io.copied[i], io.in));
+    }
+    int rc = KNN_OK;
+    for (uint32_t i = 0; i < chunks && rc == KNN_OK; ++i) {
+        const size_t first = static_cast<size_t>(i) * per, n = std::min<size_t>(per, count - first);
+        KNN_TRY_CUDA(cudaStreamWaitEvent(s, io.copied[i], 0));
+        knn::QueryArgs a{dq + first * index->dims, static_cast<uint32_t>(n), max_distance2, nullptr, k,
+                         di + first * k, dd + first * k, nullptr};
+        rc = run_query(index, a, opts, s);
+        if (rc != KNN_OK) break;
+        KNN_TRY_CUDA(cudaEventRecord(io.answered[i], s));
+        KNN_TRY_CUDA(cudaStreamWaitEvent(io.out, io.answered[i], 0));
+        KNN_TRY_CUDA(cudaMemcpyAsync(h_indexes + first * k, di + first * k, n * rrow, cudaMemcpyDeviceToHost, io.out));
+        KNN_TRY_CUDA(cudaMemcpyAsync(h_distances + first * k, dd + first * k, n * rrow, cudaMemcpyDeviceToHost,
+                                     io.out));
+    }
+    // Whatever happened, the caller's stream must not run ahead of the copies still in flight.
+    KNN_TRY_CUDA(cudaEventRecord(io.finish, io.out));
+    KNN_TRY_CUDA(cudaStreamWaitEvent(s, io.finish, 0));
+    KNN_TRY_CUDA(cudaEventRecord(io.finish, io.in));
+    KNN_TRY_CUDA(cudaStreamWaitEvent(s, io.finish, 0));
     KNN_TRY_CUDA(cudaStreamSynchronize(s));
-    return KNN_OK;
+    return rc;
 }
 
 int knn_query_stats(knn_index* index, const float* d_queries, uint32_t count, float max_distance2, uint32_t k,
@@ -501,6 +563,7 @@ int knn_query_stats(knn_index* index, const float* d_queries, uint32_t count, fl
     out->leaves_visited = hc.leaves;
     out->points_scanned = hc.points;
     out->fallback_queries = hc.fallback;
+    out->filter_give_ups = static_cast<uint64_t>(hc.give_ups);
     if (hc.error) return fail(KNN_ERR_DEVICE_LIMIT, "a query kernel's stack bound check fired");
     return KNN_OK;
 }
@@ -510,7 +573,13 @@ int knn_last_query_timing(knn_index* index, float* total_ms, float* kernel_ms) {
     if (!index->timing.valid) return fail(KNN_ERR_INVALID_ARGUMENT, "no timed query on this index");
     KNN_TRY_CUDA(cudaEventSynchronize(index->timing.total1));
     KNN_TRY_CUDA(cudaEventElapsedTime(total_ms, index->timing.total0, index->timing.total1));
-    KNN_TRY_CUDA(cudaEventElapsedTime(kernel_ms, index->timing.kern0, index->timing.kern1));
+    float sum = 0.0f;
+    for (int i = 0; i < index->timing.spans; ++i) {
+        float v = 0.0f;
+        KNN_TRY_CUDA(cudaEventElapsedTime(&v, index->timing.span[i][0], index->timing.span[i][1]));
+        sum += v;
+    }
+    *kernel_ms = sum;
     return KNN_OK;
 }
 
@@ -525,7 +594,7 @@ int knn_tuned_plan(const knn_index* index, uint32_t k, uint32_t learned_radius, 
     out->shmem_tracking = slot.plan.sh_nn;
     out->shmem_stack = slot.plan.sh_stack;
     out->leaf_scan = slot.plan.leaf_scan;
-    out->traversal = slot.plan.warp ? 1u : 0u;
+    out->traversal = slot.plan.group ? 2u : (slot.plan.warp ? 1u : 0u);
     out->flags = slot.plan.bf16 ? KNN_QF_BF16_FILTER : 0u;
     out->reserved = slot.candidates;
     if (ms) *ms = slot.ms;

@@ -248,10 +248,10 @@ static int launch_kd(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, c
     p.out_idx = a.out_idx;
     p.out_dist = a.out_dist;
     p.counters = a.counters;
-    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern0, s));
+    if (plan.timing) KNN_TRY(ix->timing.begin(s));
     kern<<<ceil_div(a.count, block), block, smem, s>>>(p);
     KNN_LAUNCHED();
-    if (plan.timing) KNN_TRY_CUDA(cudaEventRecord(ix->timing.kern1, s));
+    if (plan.timing) KNN_TRY(ix->timing.end(s));
     return KNN_OK;
 }
 
@@ -300,9 +300,14 @@ int kd_order_dp(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_
 }
 
 template <uint32_t DP>
+int kd_group_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order,
+                      float* seeds, uint32_t* fb_list, uint32_t* fb_count, cudaStream_t s);
+
+template <uint32_t DP>
 int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s) {
     const uint32_t* order = a.order;
     if (!order && p.reorder && a.count >= 4096) KNN_TRY(kd_order_dp<DP>(ix, a, s, &order));
+    if (p.group && !a.count_dev) return kd_group_query_dp<DP>(ix, a, p, order, nullptr, nullptr, nullptr, s);
     switch (k_class(a.k)) {
         case 8: return launch_kd_variant<DP, 8>(ix, a, p, order, s);
         case 16: return launch_kd_variant<DP, 16>(ix, a, p, order, s);
@@ -312,7 +317,451 @@ int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStrea
     }
 }
 
+// ---- warp-group search ---------------------------------------------------------------------------
+//
+// The 32 lanes of a warp hold 32 neighbouring queries (locality order) and a radius each (a seed
+// from the radius model or from the query's own subtree, never below its k-th distance for most
+// queries).  The warp walks the tree once for all of them, bounding every node by the distance
+// from each lane's query to the node's tight bounding box; a node is entered when some lane's
+// bound is within that lane's radius.  Leaf buckets are collected as (bucket, lanes) entries,
+// and the (bucket, query) pairs are then dealt out over the warp's lanes one pair per lane, so a
+// warp does the sum of its queries' bucket scans rather than their union.  A point within its
+// query's radius is appended to that query's candidate list in shared memory; at the end each
+// lane sorts its query's list.  A query with fewer than k candidates inside a radius below the
+// caller's grows its radius (x4 squared) and walks again; one whose list overflows, or that is
+// still short after a few rounds, goes to a list that the per-thread search answers.  Every
+// answer is exact: a bucket is skipped only when its box bound exceeds the radius, and the box
+// bound is a rigorous lower bound on the float distance of every point inside (below).
+constexpr uint32_t kGroupWarps = 4;
+constexpr uint32_t kGroupList = 64;   // bucket entries collected before they are scanned
+constexpr uint32_t kGroupStack = 40;  // node stack (the walk holds at most depth + 1 entries)
+constexpr uint32_t kGroupRounds = 4;  // radius growth rounds before the per-thread fallback
+
+__host__ __device__ constexpr uint32_t group_cap(int kmax) { return kmax <= 8 ? 32u : (kmax <= 16 ? 64u : 96u); }
+__host__ __device__ constexpr int box_qs(int dp) { return dp < 4 ? 4 : dp; }
+
+template <int DP, int KMAX>
+struct GroupWarpSmem {
+    uint64_t buf[group_cap(KMAX)][32];  // candidate keys, slot-major (slot i of lane l at [i][l])
+    uint64_t list[kGroupList];          // (bucket node << 32) | lanes
+    float qv[32][box_qs(DP)];           // the warp's queries
+    float rad[32];                      // radius of each lane this round (-1: none)
+    uint32_t cnt[32];                   // candidates appended per lane
+    uint32_t pre[32];                   // inclusive prefix of pairs per list entry
+    uint32_t stack[kGroupStack];
+};
+
+template <int DP, int KMAX>
+constexpr size_t group_smem_bytes() { return kGroupWarps * sizeof(GroupWarpSmem<DP, KMAX>); }
+
+struct KdGroupParams {
+    KdParams p;              // tree, queries, locality order, caller's radius (max_d2 / radii), outputs
+    const float* box;        // per node (depth <= box depth): lo[box_qs(DP)], hi[box_qs(DP)]
+    float* seeds;            // per query radius to start from (<= the caller's); fallback radius on exit
+    uint32_t* fb_list;       // queries left to the per-thread search
+    uint32_t* fb_count;
+    uint32_t box_stride;     // floats per box
+};
+
+// Lower bound on the float dist2 from q to any point of the box (lo, hi): per dimension the gap
+// o = max(fl(lo - q), fl(q - hi), 0), then the same fused sum as dist2 in dimension order.  For a
+// point p of the box, |fl(q - p)| >= o (p lies beyond lo or hi, and rounding is monotone), and
+// fma(t, t, acc) is non-decreasing in |t| and acc >= 0, so the bound never exceeds dist2(q, p).
+// An empty box (lo = +inf, hi = -inf) gives +inf.
+template <int DP>
+__device__ __forceinline__ float box_bound(const float (&q)[DP], const float* __restrict__ box) {
+    constexpr int QS = box_qs(DP);
+    const float4* lo4 = reinterpret_cast<const float4*>(box);
+    const float4* hi4 = reinterpret_cast<const float4*>(box + QS);
+    float acc = 0.0f;
+#pragma unroll
+    for (int v = 0; v < (DP + 3) / 4; ++v) {
+        const float4 lo = __ldg(lo4 + v), hi = __ldg(hi4 + v);
+        const float l[4] = {lo.x, lo.y, lo.z, lo.w};
+        const float h[4] = {hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (4 * v + c < DP) {
+                const float o = fmaxf(fmaxf(__fsub_rn(l[c], q[4 * v + c]), __fsub_rn(q[4 * v + c], h[c])), 0.0f);
+                acc = __fmaf_rn(o, o, acc);
+            }
+        }
+    }
+    return acc;
+}
+
+// Position of the n-th (0-based) set bit of m (n < popc(m)), by halving on popcounts.
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t w = 16; w; w >>= 1) {
+        const uint32_t c = __popc(m & ((1u << w) - 1u));
+        if (n >= c) {
+            n -= c;
+            m >>= w;
+            pos += w;
+        }
+    }
+    return pos;
+}
+
+template <int DP, int KMAX>
+__global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGroupParams gp) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using Sm = GroupWarpSmem<DP, KMAX>;
+    constexpr uint32_t C = group_cap(KMAX);
+    constexpr int QS = box_qs(DP);
+    constexpr uint32_t FULL = 0xFFFFFFFFu;
+    Sm& sm = reinterpret_cast<Sm*>(smem_raw)[threadIdx.x >> 5];
+    const KdParams& p = gp.p;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t g = (blockIdx.x * kGroupWarps + (threadIdx.x >> 5)) * 32u;
+    if (g >= p.nq) return;  // whole warp idle; warps never wait on one another
+    const uint32_t t = g + lane;
+    const bool active = t < p.nq;
+    const uint32_t qi = active ? (p.order ? p.order[t] : t) : 0u;
+    float q[DP];
+    load_query<DP>(p.queries, p.dims, qi, q);
+#pragma unroll
+    for (int d = 0; d < QS; ++d) sm.qv[lane][d] = d < DP ? q[d] : 0.0f;
+    const float R = active ? (p.radii ? p.radii[qi] : p.max_d2) : -1.0f;
+    float r = active ? gp.seeds[qi] : -1.0f;
+    if (!(r <= R)) r = R;  // a seed above the caller's radius (or NaN) starts at the caller's
+    bool pending = active;
+    const uint32_t stop = p.stop_depth;
+    const uint32_t bucket_slots = p.leaf_slots << (p.node_depth - stop);
+    uint32_t nodes = 0, pairs = 0;
+    bool stack_error = false;
+
+    // Scans the collected (bucket, lanes) entries, one (bucket, query) pair per lane at a time.
+    auto scan = [&](uint32_t n) {
+        for (uint32_t base = 0; base < n; base += 32) {
+            const uint32_t e = base + lane;
+            const uint32_t m = e < n ? static_cast<uint32_t>(sm.list[e]) : 0u;
+            uint32_t incl = __popc(m);
+#pragma unroll
+            for (uint32_t o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const uint32_t total = __shfl_sync(FULL, incl, 31);
+            sm.pre[lane] = incl;
+            __syncwarp();
+            for (uint32_t it = lane; it < total; it += 32) {
+                uint32_t j = 0;  // first entry whose inclusive prefix exceeds it
+#pragma unroll
+                for (uint32_t step = 16; step; step >>= 1)
+                    if (sm.pre[j + step - 1] <= it) j += step;
+                const uint64_t ent = sm.list[base + j];
+                const uint32_t excl = j ? sm.pre[j - 1] : 0u;
+                const uint32_t ql = nth_set_bit(static_cast<uint32_t>(ent), it - excl);
+                float qq[DP];
+#pragma unroll
+                for (int d = 0; d < DP; ++d) qq[d] = sm.qv[ql][d];
+                const float rq = sm.rad[ql];
+                const SlotRange sr = subtree_slots(static_cast<uint32_t>(ent >> 32), stop, p.node_depth, p.node_count,
+                                                   p.leaf_slots);
+                const float* slot = p.leaf + sr.first * p.leaf_stride;
+#pragma unroll 4
+                for (uint32_t s = 0; s < bucket_slots; ++s, slot += p.leaf_stride) {
+                    int32_t id;
+                    const float d2 = slot_dist<DP>(qq, slot, &id);
+                    if (id >= 0 && d2 <= rq) {
+                        const uint32_t pos = atomicAdd(&sm.cnt[ql], 1u);
+                        if (pos < C) sm.buf[pos][ql] = make_key(d2, id);
+                    }
+                }
+                ++pairs;
+            }
+            __syncwarp();
+        }
+    };
+
+    for (uint32_t round = 0; __any_sync(FULL, pending); ++round) {
+        const float rl = pending ? r : -1.0f;
+        sm.cnt[lane] = 0;
+        sm.rad[lane] = rl;
+        __syncwarp();
+        uint32_t top = 0, nlist = 0;
+        const uint32_t m0 = __ballot_sync(FULL, box_bound<DP>(q, gp.box) <= rl);
+        if (m0) {
+            if (stop == 0) {
+                if (lane == 0) sm.list[0] = m0;
+                nlist = 1;
+            } else {
+                if (lane == 0) sm.stack[0] = 0;
+                top = 1;
+            }
+        }
+        while (top) {
+            __syncwarp();
+            const uint32_t node = sm.stack[--top];
+            const uint32_t l = 2 * node + 1;
+            const float bl = box_bound<DP>(q, gp.box + static_cast<size_t>(l) * gp.box_stride);
+            const float br = box_bound<DP>(q, gp.box + static_cast<size_t>(l + 1) * gp.box_stride);
+            const uint32_t ml = __ballot_sync(FULL, bl <= rl);
+            const uint32_t mr = __ballot_sync(FULL, br <= rl);
+            ++nodes;
+            if (heap_depth(node) + 1 == stop) {
+                if (lane == 0) {
+                    if (ml) sm.list[nlist] = (static_cast<uint64_t>(l) << 32) | ml;
+                    if (mr) sm.list[nlist + (ml ? 1 : 0)] = (static_cast<uint64_t>(l + 1) << 32) | mr;
+                }
+                nlist += (ml ? 1u : 0u) + (mr ? 1u : 0u);
+                if (nlist + 2 > kGroupList) {
+                    __syncwarp();
+                    scan(nlist);
+                    nlist = 0;
+                }
+            } else {
+                if (top + 2 > kGroupStack) {  // cannot happen (at most one entry per level); recorded
+                    stack_error = true;
+                    continue;
+                }
+                if (lane == 0) {
+                    if (mr) sm.stack[top] = l + 1;
+                    if (ml) sm.stack[top + (mr ? 1 : 0)] = l;
+                }
+                top += (ml ? 1u : 0u) + (mr ? 1u : 0u);
+            }
+        }
+        if (nlist) {
+            __syncwarp();
+            scan(nlist);
+        }
+        __syncwarp();
+        if (pending) {
+            const uint32_t c = sm.cnt[lane];
+            if (c > C) {
+                // More candidates than the list holds: at least k lie within r, so the per-thread
+                // search with radius r answers exactly.
+                const uint32_t pos = atomicAdd(gp.fb_count, 1u);
+                gp.fb_list[pos] = qi;
+                gp.seeds[qi] = r;
+                if (p.counters) atomicAdd(&p.counters->fallback, 1ull);
+                pending = false;
+            } else if (c >= p.k || !(r < R)) {
+                Tracker<KMAX, false, false> tr;
+                tr.init(p.k, R, nullptr, 0);
+                for (uint32_t i = 0; i < c; ++i) tr.offer(sm.buf[i][lane]);
+                tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
+                pending = false;
+            } else if (round + 1 >= kGroupRounds) {
+                const uint32_t pos = atomicAdd(gp.fb_count, 1u);
+                gp.fb_list[pos] = qi;
+                gp.seeds[qi] = R;
+                if (p.counters) atomicAdd(&p.counters->fallback, 1ull);
+                pending = false;
+            } else {
+                r = fminf(R, fmaxf(r * 4.0f, 1e-30f));
+            }
+        }
+        __syncwarp();
+    }
+    if (p.counters) {
+        // nodes: popped nodes (each tests its two children); leaves: (bucket, query) pairs.
+        if (lane == 0) {
+            atomicAdd(&p.counters->nodes, static_cast<unsigned long long>(nodes));
+            if (stack_error) atomicExch(&p.counters->error, 1);
+        }
+        if (pairs) {
+            atomicAdd(&p.counters->leaves, static_cast<unsigned long long>(pairs));
+            atomicAdd(&p.counters->points, static_cast<unsigned long long>(pairs) * bucket_slots);
+        }
+    }
+}
+
+// Per-thread search of the queries the group search left over (grid-stride over the list).
+template <int DP, int KMAX>
+__global__ void __launch_bounds__(128) kd_fallback_kernel(const KdParams p) {
+    const uint32_t n = *p.count_dev;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        kd_search_thread<DP, KMAX, false, false, false>(p, t, nullptr);
+}
+
+// Self seeds: each query's k-th distance among the points of the subtree of at least
+// max(4k, 32) slots it descends to -- an upper bound on its k-th neighbour distance (those
+// points are real points), capped by the caller's radius.  The caller's radius where the
+// subtree holds fewer than k points.
+template <int DP, int KMAX>
+__global__ void __launch_bounds__(128) kd_self_seed_kernel(const KdParams p, uint32_t seed_depth, float* __restrict__ seeds) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.nq) return;
+    const uint32_t qi = p.order ? p.order[t] : t;
+    float q[DP];
+    load_query<DP>(p.queries, p.dims, qi, q);
+    const float R = p.radii ? p.radii[qi] : p.max_d2;
+    uint32_t node = 0;
+    for (uint32_t depth = 0; depth < seed_depth; ++depth) {
+        const float diff = pick<DP>(q, depth % p.aux) - __ldg(p.split + node);
+        node = 2 * node + (diff < 0.0f ? 1u : 2u);
+    }
+    Tracker<KMAX, false, false> tr;
+    tr.init(p.k, R, nullptr, 0);
+    const SlotRange sr = subtree_slots(node, seed_depth, p.node_depth, p.node_count, p.leaf_slots);
+    const float* slot = p.leaf + sr.first * p.leaf_stride;
+    for (uint32_t s = 0; s < sr.count; ++s, slot += p.leaf_stride) {
+        int32_t id;
+        const float d2 = slot_dist<DP>(q, slot, &id);
+        if (id >= 0) tr.offer(make_key(d2, id));
+    }
+    seeds[qi] = tr.radius();  // the caller's radius while fewer than k points were offered
+}
+
+// Tight boxes of the nodes down to `depth` (per node lo[QS], hi[QS]; padding slots excluded).
+template <int DP>
+__global__ void kd_box_bottom_kernel(const float* __restrict__ leaf, uint32_t leaf_stride, uint32_t depth,
+                                     uint32_t node_depth, uint32_t node_count, uint32_t leaf_slots,
+                                     float* __restrict__ box, uint32_t box_stride) {
+    constexpr int QS = box_qs(DP);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (1u << depth)) return;
+    const uint32_t node = (1u << depth) - 1u + i;
+    float lo[QS], hi[QS];
+#pragma unroll
+    for (int d = 0; d < QS; ++d) {
+        lo[d] = d < DP ? INFINITY : 0.0f;
+        hi[d] = d < DP ? -INFINITY : 0.0f;
+    }
+    const SlotRange sr = subtree_slots(node, depth, node_depth, node_count, leaf_slots);
+    const float* slot = leaf + sr.first * leaf_stride;
+    for (uint32_t s = 0; s < sr.count; ++s, slot += leaf_stride) {
+        if (__float_as_int(slot[DP]) < 0) continue;  // padding
+#pragma unroll
+        for (int d = 0; d < DP; ++d) {
+            lo[d] = fminf(lo[d], slot[d]);
+            hi[d] = fmaxf(hi[d], slot[d]);
+        }
+    }
+    float* out = box + static_cast<size_t>(node) * box_stride;
+#pragma unroll
+    for (int d = 0; d < QS; ++d) {
+        out[d] = lo[d];
+        out[QS + d] = hi[d];
+    }
+}
+
+template <int QS>
+__global__ void kd_box_up_kernel(float* __restrict__ box, uint32_t depth) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (1u << depth)) return;
+    const uint32_t node = (1u << depth) - 1u + i;
+    const float* a = box + static_cast<size_t>(2 * node + 1) * (2 * QS);
+    const float* b = a + 2 * QS;
+    float* out = box + static_cast<size_t>(node) * (2 * QS);
+#pragma unroll
+    for (int d = 0; d < QS; ++d) {
+        out[d] = fminf(a[d], b[d]);
+        out[QS + d] = fmaxf(a[QS + d], b[QS + d]);
+    }
+}
+
+template <uint32_t DP>
+int kd_box_build_dp(knn_index* ix, cudaStream_t s) {
+    constexpr uint32_t QS = box_qs(DP);
+    const uint32_t depth = ix->kd_box_depth;
+    const size_t nodes = (static_cast<size_t>(2) << depth) - 1;
+    ix->kd_box_stride = 2 * QS;
+    KNN_TRY(ix->kd_box.alloc(nodes * ix->kd_box_stride * sizeof(float)));
+    kd_box_bottom_kernel<DP><<<ceil_div(1u << depth, 256), 256, 0, s>>>(
+        ix->leaf.as<float>(), ix->leaf_stride, depth, ix->node_depth, ix->node_count, ix->leaf_slots,
+        ix->kd_box.as<float>(), ix->kd_box_stride);
+    KNN_LAUNCHED();
+    for (uint32_t d = depth; d-- > 0;) {
+        kd_box_up_kernel<QS><<<ceil_div(1u << d, 256), 256, 0, s>>>(ix->kd_box.as<float>(), d);
+        KNN_LAUNCHED();
+    }
+    return KNN_OK;
+}
+
+template <int DP, int KMAX>
+static int launch_kd_group(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order,
+                           float* seeds, bool self_seed, uint32_t* fb_list, uint32_t* fb_count, cudaStream_t s) {
+    KdGroupParams gp{};
+    KdParams& p = gp.p;
+    p.split = ix->split.as<float>();
+    p.leaf = ix->leaf.as<float>();
+    p.leaf_stride = ix->leaf_stride;
+    p.node_count = ix->node_count;
+    p.node_depth = ix->node_depth;
+    p.stop_depth = scan_depth_for(ix->node_depth, ix->leaf_slots, plan.leaf_scan ? plan.leaf_scan : 8u);
+    if (p.stop_depth > ix->kd_box_depth) p.stop_depth = ix->kd_box_depth;
+    p.leaf_slots = ix->leaf_slots;
+    p.aux = ix->aux_dims;
+    p.queries = a.queries;
+    p.dims = ix->dims;
+    p.nq = a.count;
+    p.order = order;
+    p.max_d2 = a.max_d2;
+    p.radii = a.radii;
+    p.k = a.k;
+    p.out_idx = a.out_idx;
+    p.out_dist = a.out_dist;
+    p.counters = a.counters;
+    gp.box = ix->kd_box.as<float>();
+    gp.box_stride = ix->kd_box_stride;
+    gp.seeds = seeds;
+    gp.fb_list = fb_list;
+    gp.fb_count = fb_count;
+    KNN_TRY_CUDA(cudaMemsetAsync(fb_count, 0, sizeof(uint32_t), s));
+    if (self_seed) {
+        // Subtree of at least max(4k, 32) slots.
+        const uint32_t want = std::max<uint32_t>(32u, 4u * a.k);
+        uint32_t sd = ix->node_depth;
+        while (sd > 0 && (static_cast<uint64_t>(ix->leaf_slots) << (ix->node_depth - sd)) < want) --sd;
+        kd_self_seed_kernel<DP, KMAX><<<ceil_div(a.count, 128), 128, 0, s>>>(p, sd, seeds);
+        KNN_LAUNCHED();
+    }
+    constexpr size_t smem = group_smem_bytes<DP, KMAX>();
+    auto kern = kd_group_kernel<DP, KMAX>;
+    KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    if (plan.timing) KNN_TRY(ix->timing.begin(s));
+    kern<<<ceil_div(a.count, 32 * kGroupWarps), 32 * kGroupWarps, smem, s>>>(gp);
+    KNN_LAUNCHED();
+    KdParams fp = p;
+    fp.order = fb_list;
+    fp.count_dev = fb_count;
+    fp.radii = seeds;
+    kd_fallback_kernel<DP, KMAX><<<2 * static_cast<uint32_t>(sm_count()), 128, 0, s>>>(fp);
+    KNN_LAUNCHED();
+    if (plan.timing) KNN_TRY(ix->timing.end(s));
+    return KNN_OK;
+}
+
+// Warp-group search (plan.group) with per-query seeds (or self seeds when `seeds` holds none):
+// boxes built on first use, locality order, the group kernel and the fallback list.  Scratch
+// (seeds when self-seeded, the fallback list) comes from the index workspace after the order.
+template <uint32_t DP>
+int kd_group_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order,
+                      float* seeds, uint32_t* fb_list, uint32_t* fb_count, cudaStream_t s) {
+    if constexpr (DP > 16) {
+        return fail(KNN_ERR_INVALID_ARGUMENT, "group search: dims above 16");
+    } else {
+        if (a.k > 32) return fail(KNN_ERR_INVALID_ARGUMENT, "group search: k above 32");
+        if (!ix->kd_box.ptr) {
+            ix->kd_box_depth = scan_depth_for(ix->node_depth, ix->leaf_slots, 4);
+            KNN_TRY(kd_box_build_dp<DP>(ix, s));
+        }
+        const bool self_seed = seeds == nullptr;
+        const size_t n = a.count;
+        if (self_seed) {
+            KNN_TRY(ix->group_ws.reserve(carve_bytes({n * 4, n * 4, 256})));
+            Carver c(ix->group_ws.ptr);
+            seeds = c.take<float>(n);
+            fb_list = c.take<uint32_t>(n);
+            fb_count = c.take<uint32_t>(1);
+        }
+        switch (k_class(a.k)) {
+            case 8: return launch_kd_group<DP, 8>(ix, a, plan, order, seeds, self_seed, fb_list, fb_count, s);
+            case 16: return launch_kd_group<DP, 16>(ix, a, plan, order, seeds, self_seed, fb_list, fb_count, s);
+            default: return launch_kd_group<DP, 32>(ix, a, plan, order, seeds, self_seed, fb_list, fb_count, s);
+        }
+    }
+}
+
 template int kd_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
+template int kd_group_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, float*,
+                                        uint32_t*, uint32_t*, cudaStream_t);
 template int kd_order_dp<KNN_DP>(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
 
 

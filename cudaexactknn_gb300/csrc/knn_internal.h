@@ -148,7 +148,8 @@ struct DevCounters {
     unsigned long long points;
     unsigned long long fallback;
     int error;      // a kernel's bounds check fired
-    int pad[7];
+    int give_ups;   // tensor-core filter blocks that gave up (bounded waits ran out)
+    int pad[6];
 };
 
 // ---- the index ----------------------------------------------------------------------------------
@@ -160,22 +161,108 @@ struct QueryPlan {
     bool reorder = true;
     bool timing = false;     // record events around the main search kernel
     bool warp = false;       // trees: warp-coherent traversal instead of one search per thread
+    bool group = false;      // k-d tree: warp-group search from per-query radii (traversal 2)
     bool bf16 = false;       // brute force: BF16 tensor-core filter + FP32 rescoring
     uint32_t tc_cap = 0;     // candidates kept per query by the filter (0 = default)
     uint32_t leaf_scan = 0;  // 0 = tree leaves
+    bool test_give_up = false;  // tensor-core filter blocks give up after their first copy (tests)
 };
 
-// Events bracketing a query and its main search kernel (KNN_QF_TIMING).
+// Events bracketing a query and each of its search kernels (KNN_QF_TIMING).  A learned-radius
+// query runs its seeded search and up to three retry searches: every one of them records a
+// span, and the kernel time is the sum of the spans.
 struct QueryTiming {
-    cudaEvent_t total0 = nullptr, total1 = nullptr, kern0 = nullptr, kern1 = nullptr;
+    static constexpr int kMaxSpans = 8;
+    cudaEvent_t total0 = nullptr, total1 = nullptr;
+    cudaEvent_t span[kMaxSpans][2] = {};
+    int spans = 0;
     bool valid = false;
     ~QueryTiming() {
-        for (cudaEvent_t e : {total0, total1, kern0, kern1})
+        for (cudaEvent_t e : {total0, total1})
             if (e) cudaEventDestroy(e);
+        for (auto& p : span)
+            for (cudaEvent_t e : p)
+                if (e) cudaEventDestroy(e);
     }
     int ensure() {
         if (total0) return KNN_OK;
-        for (cudaEvent_t* e : {&total0, &total1, &kern0, &kern1}) KNN_TRY_CUDA(cudaEventCreate(e));
+        KNN_TRY_CUDA(cudaEventCreate(&total0));
+        KNN_TRY_CUDA(cudaEventCreate(&total1));
+        for (auto& p : span)
+            for (cudaEvent_t& e : p) KNN_TRY_CUDA(cudaEventCreate(&e));
+        return KNN_OK;
+    }
+    // Opens / closes the span of one search kernel on stream s (spans past kMaxSpans are merged
+    // into the last one).
+    int begin(cudaStream_t s) {
+        if (spans < kMaxSpans) KNN_TRY_CUDA(cudaEventRecord(span[spans][0], s));
+        return KNN_OK;
+    }
+    int end(cudaStream_t s) {
+        const int i = spans < kMaxSpans ? spans : kMaxSpans - 1;
+        KNN_TRY_CUDA(cudaEventRecord(span[i][1], s));
+        if (spans < kMaxSpans) ++spans;
+        return KNN_OK;
+    }
+};
+
+// Device-side ordering of the queries issued on one index: they share its workspaces, so a query
+// issued on another stream than the previous one waits (on the device) for the previous one to
+// finish.  Skipped while the stream is being captured into a graph.
+struct StreamOrder {
+    cudaEvent_t done = nullptr;
+    cudaStream_t last = nullptr;
+    bool used = false;
+    ~StreamOrder() {
+        if (done) cudaEventDestroy(done);
+    }
+    int before(cudaStream_t s) {
+        if (!used || s == last) return KNN_OK;
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        KNN_TRY_CUDA(cudaStreamIsCapturing(s, &cs));
+        if (cs == cudaStreamCaptureStatusNone) KNN_TRY_CUDA(cudaStreamWaitEvent(s, done, 0));
+        return KNN_OK;
+    }
+    int after(cudaStream_t s) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        KNN_TRY_CUDA(cudaStreamIsCapturing(s, &cs));
+        if (cs != cudaStreamCaptureStatusNone) return KNN_OK;
+        if (!done) KNN_TRY_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+        KNN_TRY_CUDA(cudaEventRecord(done, s));
+        last = s;
+        used = true;
+        return KNN_OK;
+    }
+};
+
+// knn_query_host's copy pipeline: queries are answered in chunks; chunk i+1's queries are copied
+// in on `in` while chunk i is searched on the caller's stream and chunk i-1's rows are copied out
+// on `out`.
+struct HostIo {
+    static constexpr int kMaxChunks = 8;
+    cudaStream_t in = nullptr, out = nullptr;
+    cudaEvent_t start = nullptr, finish = nullptr;
+    cudaEvent_t copied[kMaxChunks] = {}, answered[kMaxChunks] = {};
+    ~HostIo() {
+        for (cudaEvent_t e : {start, finish})
+            if (e) cudaEventDestroy(e);
+        for (int i = 0; i < kMaxChunks; ++i) {
+            if (copied[i]) cudaEventDestroy(copied[i]);
+            if (answered[i]) cudaEventDestroy(answered[i]);
+        }
+        if (in) cudaStreamDestroy(in);
+        if (out) cudaStreamDestroy(out);
+    }
+    int ensure() {
+        if (in) return KNN_OK;
+        KNN_TRY_CUDA(cudaStreamCreateWithFlags(&in, cudaStreamNonBlocking));
+        KNN_TRY_CUDA(cudaStreamCreateWithFlags(&out, cudaStreamNonBlocking));
+        KNN_TRY_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+        KNN_TRY_CUDA(cudaEventCreateWithFlags(&finish, cudaEventDisableTiming));
+        for (int i = 0; i < kMaxChunks; ++i) {
+            KNN_TRY_CUDA(cudaEventCreateWithFlags(&copied[i], cudaEventDisableTiming));
+            KNN_TRY_CUDA(cudaEventCreateWithFlags(&answered[i], cudaEventDisableTiming));
+        }
         return KNN_OK;
     }
 };
@@ -222,6 +309,12 @@ struct knn_index {
 
     // k-d tree: split value per internal node (implicit heap, children 2i+1, 2i+2).
     knn::DevBuf split;
+    // k-d tree, warp-group search (built on first use): the tight bounding box of the points
+    // under every node down to depth kd_box_depth (subtrees of at most 4 slots), per node
+    // lo[q], hi[q] with q = max(4, padded dims) floats each; and the search's own scratch.
+    knn::DevBuf kd_box;
+    uint32_t kd_box_depth = 0, kd_box_stride = 0;
+    knn::DevBuf group_ws;
 
     // Trees: leaf slots, 2^node_depth leaves x leaf_slots slots; a slot is `leaf_stride` floats:
     // coordinates (dp, zero padded) then the point index as int32 bits (-1 = empty slot).
@@ -240,6 +333,8 @@ struct knn_index {
     // Scratch for queries, grown on demand, reused across calls.
     knn::DevBuf workspace;
     knn::DevBuf staging;   // device copies of host queries/results (knn_query_host)
+    knn::HostIo host_io;   // knn_query_host's copy streams
+    knn::StreamOrder order_guard;
     knn::DevBuf counters;  // DevCounters
     knn::QueryTiming timing;
 
@@ -318,6 +413,10 @@ int tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* bad);
 int kd_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order);
 int ball_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order);
 int kd_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
+// Warp-group k-d search from per-query seed radii (kd_kernels.cu); queries it cannot settle go to
+// fb_list / fb_count and are answered by the per-thread search in the same call.
+int kd_group_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, const uint32_t* order, float* seeds,
+                   uint32_t* fb_list, uint32_t* fb_count, cudaStream_t s);
 int ball_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 
 // Rows of unfilled results (index -1, distance = radius) for an empty point set.

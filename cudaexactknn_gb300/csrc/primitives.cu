@@ -4,6 +4,7 @@
 // The reference sorts with cub::DeviceRadixSort and scans with cub::DeviceScan
 // (src/KdTreeGpu.cuh:313-320, src/BallTreeGpu.cuh:500-505); the engine uses these instead.
 
+#include <atomic>
 #include "knn_internal.h"
 
 namespace knn {
@@ -208,14 +209,19 @@ int fill_empty_rows(const QueryArgs& a, cudaStream_t s) {
 }
 
 int sm_count() {
-    static int cached = 0;
-    if (cached == 0) {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
+    // Cached per device ordinal: a process may query indexes on GPUs of different sizes.
+    constexpr int kDevices = 64;
+    static std::atomic<int> cached[kDevices];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int slot = dev >= 0 && dev < kDevices ? dev : 0;
+    int v = cached[slot].load(std::memory_order_relaxed);
+    if (v == 0) {
         cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        cached = v > 0 ? v : 1;
+        v = v > 0 ? v : 1;
+        cached[slot].store(v, std::memory_order_relaxed);
     }
-    return cached;
+    return v;
 }
 
 }  // namespace knn

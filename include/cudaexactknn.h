@@ -36,7 +36,10 @@
  *   - a negative or NaN max_distance2, k == 0 or dims == 0 is KNN_ERR_INVALID_ARGUMENT.
  *
  * Supported sizes: 1 <= dims <= 128, 1 <= k <= 128, n < 2^31, count < 2^31.
- * One query at a time per index: an index owns one scratch workspace.
+ * Streams: an index owns one scratch workspace, so its queries run one after another on the
+ * device.  A query issued on another stream than the index's previous query waits (an event on
+ * the device, no host synchronisation) for that query to finish; different indexes on different
+ * streams run concurrently.  Calls on one index come from one host thread at a time.
  */
 #ifndef CUDAEXACTKNN_H
 #define CUDAEXACTKNN_H
@@ -81,7 +84,12 @@ typedef enum knn_structure {
                                     FP16's range) tcgen05 filter with rigorous bounds + exact FP32
                                     rescore; the same answer as the plain search */
 #define KNN_QF_KEEP_ORDER 16u    /* do not reorder queries for locality */
-#define KNN_QF_TIMING 32u        /* record CUDA events around the query and its search kernel */
+#define KNN_QF_TIMING 32u        /* record CUDA events around the query and each of its search kernels */
+/* Test only: every tensor-core filter block gives up right after issuing its first point-tile
+ * copy, as it does when one of its bounded waits runs out: it drains what it issued, frees its
+ * tensor memory, flags the error, and leaves its queries (and the tiles it never took) to the
+ * exhaustive search, so the answers are unchanged. */
+#define KNN_QF_TEST_FILTER_GIVE_UP 0x40000000u
 
 /*
  * Run-time form of batchKnn's template arguments (src/KdTreeGpu.cuh:392,
@@ -98,7 +106,12 @@ typedef struct knn_query_opts {
     uint32_t leaf_scan;     /* trees: scan whole subtrees of at most this many points as one
                                leaf (0 = the tree's own leaves) */
     uint32_t traversal;     /* trees: 0 = one depth-first search per thread (the reference's
-                               scheme), 1 = warp-coherent search (a warp's queries walk together) */
+                               scheme), 1 = warp-coherent search (a warp's queries walk together);
+                               k-d trees of at most 16 dims, k <= 32: 2 = warp-group search (a
+                               warp's 32 queries walk the tree once against tight node boxes from
+                               per-query radii -- the radius model's seeds, or each query's own
+                               subtree -- and share out their (bucket, query) scans; leaf_scan =
+                               points per bucket, 0 = 8) */
     uint32_t reserved;      /* KNN_QF_BF16_FILTER: candidates kept per query (0 = the engine's
                                default, min(4096, max(1024, 16 k))); for
                                knn_tuned_plan, the number of candidate plans timed */
@@ -109,8 +122,11 @@ typedef struct knn_query_counters {
     uint64_t nodes_visited;    /* internal nodes whose bound was evaluated */
     uint64_t leaves_visited;   /* leaves scanned */
     uint64_t points_scanned;   /* leaf slots whose distance was computed */
-    uint64_t fallback_queries; /* learned-radius queries re-run unbounded */
-    uint64_t reserved[4];
+    uint64_t fallback_queries; /* queries the fast form handed to the plain search: learned-
+                                  radius retries, warp-group and tensor-core filter fallbacks */
+    uint64_t filter_give_ups;  /* tensor-core filter blocks whose bounded waits ran out (their
+                                  queries are answered by the exhaustive search) */
+    uint64_t reserved[3];
 } knn_query_counters;
 
 typedef struct knn_index_info {
@@ -180,8 +196,12 @@ KNN_API int knn_query_radii(knn_index* index, const float* d_queries, uint32_t c
                     const float* d_max_distance2, uint32_t k, int32_t* d_indexes,
                     float* d_distances, const knn_query_opts* opts, void* stream);
 
-/* As knn_query with HOST buffers: copies queries in and results out on `stream` and
- * synchronises.  Pinned host memory gives full-speed copies. */
+/* As knn_query with HOST buffers, and synchronises.  Batches of at least 262,144 queries are
+ * answered in up to 8 chunks (>= 131,072 queries each) whose copies overlap the search: chunk i+1
+ * is copied in on one of the index's copy streams while chunk i is searched on `stream` and chunk
+ * i-1's rows are copied out on the other (one cudaMemcpyAsync per chunk and array).  Replaces the
+ * reference's copy, batchKnn and device-wide synchronisation (src/KdTreeGpu.cuh:394-410,
+ * src/BruteForceGpu.cuh:75-83).  Pinned host memory gives full-speed, asynchronous copies. */
 KNN_API int knn_query_host(knn_index* index, const float* h_queries, uint32_t count,
                    float max_distance2, uint32_t k, int32_t* h_indexes, float* h_distances,
                    const knn_query_opts* opts, void* stream);
@@ -236,8 +256,10 @@ KNN_API int knn_radius_model_import(knn_index* index, const float* h_params, uin
 KNN_API int knn_radius_model_gradients(const float* h_params, uint32_t dims, const float* h_x,
                                        const float* h_targets, uint32_t batch, float* h_grad, float* h_loss);
 
-/* Device time (ms) of the index's last KNN_QF_TIMING query: the whole query and its main search
- * kernel alone (CUDA events on the query's stream; waits for the query to finish). */
+/* Device time (ms) of the index's last KNN_QF_TIMING query: the whole query, and the sum of the
+ * spans of its search kernels (a learned-radius query: the seeded search and every retry search;
+ * the tensor-core filter: its filter kernel) measured by CUDA events on the query's stream.
+ * Waits for the query to finish. */
 KNN_API int knn_last_query_timing(knn_index* index, float* total_ms, float* kernel_ms);
 
 /* The plan KNN_QF_AUTOTUNE chose for this index and k (block size, tracking, storage, leaf

@@ -163,3 +163,35 @@ def test_persistent_blocks_take_several_query_tiles(structure, dims, k, nq):
     want = oracle.bf_knn(pts, qs[rows], k, fma=True, threads=8)
     gu.assert_rows_equal(idx[rows], dist[rows], *want, what=f"{structure} D={dims} k={k} nq={nq}")
     ix.close()
+
+
+@pytest.mark.parametrize("structure,dims,k,nq", [("bf", 32, 10, 700), ("bf", 128, 100, 40000), ("ball", 16, 32, 3000)])
+def test_filter_blocks_that_give_up_leave_exact_answers(structure, dims, k, nq):
+    """Every filter block gives up right after its first point-tile copy, as when one of its
+    bounded waits runs out (test flag): it drains the copies and MMAs it issued, frees its tensor
+    memory and flags the error, and the call still returns.  The give-ups are counted, every query
+    goes to the exhaustive search, and every row equals the oracle's."""
+    from cudaexactknn_gb300 import _lib, knn
+    rng = np.random.default_rng(dims * 7 + k)
+    if structure == "ball":
+        pts, basis = W.subspace(rng, 20000, dims, 4, 0.05)
+        qs, _ = W.subspace(rng, nq, dims, 4, 0.05, basis)
+    else:
+        pts, centres = W.gauss_mix(rng, 20000, dims, 32, 0.3)
+        qs, _ = W.gauss_mix(rng, nq, dims, 32, 0.3, centres)
+    ix = gu.make_index(structure, pts, 1 if structure == "ball" else None)
+    flags = _flags() | _lib.QF_TEST_FILTER_GIVE_UP
+    q = knn.Query(gu.to_dev(qs), len(qs), float("inf"))
+    c = ix.stats(q, k, flags=flags)
+    assert c.filter_give_ups >= 1
+    assert c.fallback_queries == nq, (c.fallback_queries, nq)
+    idx, dist = q.r_indexes.cpu().numpy(), q.r_distances.cpu().numpy()
+    rows = np.arange(nq) if nq <= 3000 else np.random.default_rng(2).choice(nq, size=1000, replace=False)
+    want = oracle.bf_knn(pts, qs[rows], k, fma=True, threads=8)
+    gu.assert_rows_equal(idx[rows], dist[rows], *want, what=f"give-up {structure} D={dims} k={k}")
+    # The same index answers normally afterwards (nothing left behind by the blocks that gave up).
+    c2 = ix.stats(q, k, flags=_flags())
+    assert c2.filter_give_ups == 0
+    gu.assert_rows_equal(q.r_indexes.cpu().numpy()[rows], q.r_distances.cpu().numpy()[rows], *want,
+                         what=f"after give-up {structure} D={dims} k={k}")
+    ix.close()

@@ -57,3 +57,63 @@ def test_full_size_workload(name):
     sel = torch.from_numpy(rows).to(chosen_i.device)
     gu.assert_rows_equal(chosen_i[sel].cpu().numpy(), chosen_d[sel].cpu().numpy(), *want, what=f"{name} sample")
     ix.close()
+
+
+def _same_rows(a_i, a_d, b_i, b_d, what):
+    import torch
+    assert torch.equal(a_i, b_i), f"{what}: indices differ"
+    assert torch.equal(a_d.view(torch.int32), b_d.view(torch.int32)), f"{what}: distances differ"
+
+
+def test_c5_uneven_batch_full_size():
+    """The 64 uneven sets of the batch workload at full size, in one autotuned graph launch: every
+    row of every set equals one plain knn call on that set, a second run repeats the first, and a
+    seeded sample of each set's rows equals the oracle's brute force."""
+    import torch
+    from cudaexactknn_gb300 import knn
+    sets = W.c5_sets()
+    built = [(gu.make_index(w.structure, w.points, w.depth_skips), w) for w in sets]
+    batch = knn.Batch([(ix, gu.to_dev(w.queries), w.k, w.max_dist2) for ix, w in built], autotune=True)
+    res = [(i.clone(), d.clone()) for i, d in batch.run()]
+    again = batch.run()
+    rng = np.random.default_rng(55)
+    for j, ((ix, w), (oi, od)) in enumerate(zip(built, res)):
+        _same_rows(oi, od, *again[j], f"set {j} second run")
+        pi, pd = ix.knn(gu.to_dev(w.queries), w.k, w.max_dist2)
+        torch.cuda.synchronize()
+        _same_rows(oi, od, pi, pd, f"set {j} ({w.name}) batch vs plain")
+        rows = np.sort(rng.choice(len(w.queries), size=min(16, len(w.queries)), replace=False))
+        want = oracle.bf_knn(w.points, w.queries[rows], w.k, w.max_dist2, fma=True, threads=16)
+        sel = torch.from_numpy(rows).to(oi.device)
+        gu.assert_rows_equal(oi[sel].cpu().numpy(), od[sel].cpu().numpy(), *want, what=f"set {j} oracle sample")
+    batch.close()
+    for ix, _ in built:
+        ix.close()
+
+
+@pytest.mark.parametrize("structure", ["kd", "ball", "bf"])
+def test_range_limited_full_size(structure):
+    """The reference's range-limited workload (tests/DimXSpeedTests.cu) at full size, D = 16:
+    N = 500,000, Q = 10,000, K = 5, maxDistance2 = 0.16.  The autotuned form equals the plain form
+    (the reference benchmarks' template choices) on every row; most rows are partly unfilled, and
+    unfilled slots hold (-1, maxDistance2); a sample equals the oracle."""
+    import torch
+    from cudaexactknn_gb300 import _lib
+    w = W.range_limited(1.0, 16, structure)
+    ix = gu.make_index(structure, w.points, w.depth_skips)
+    qs = gu.to_dev(w.queries)
+    plain_kw = {"kd": dict(block_size=32, shmem_stack=True),
+                "ball": dict(block_size=16, heap=True, shmem_tracking=True, shmem_stack=True),
+                "bf": dict(block_size=32)}[structure]
+    pi, pd = ix.knn(qs, w.k, w.max_dist2, **plain_kw)
+    ci, cd = ix.knn(qs, w.k, w.max_dist2, flags=_lib.QF_AUTOTUNE)
+    torch.cuda.synchronize()
+    _same_rows(ci, cd, pi, pd, f"range {structure}")
+    unfilled = ci < 0
+    assert bool(unfilled.any()), "the range-limited workload leaves slots unfilled"
+    assert bool((cd[unfilled] == float(np.float32(w.max_dist2))).all())
+    rows = np.sort(np.random.default_rng(6).choice(len(w.queries), size=SAMPLE_ROWS, replace=False))
+    want = oracle.bf_knn(w.points, w.queries[rows], w.k, w.max_dist2, fma=True, threads=16)
+    sel = torch.from_numpy(rows).to(ci.device)
+    gu.assert_rows_equal(ci[sel].cpu().numpy(), cd[sel].cpu().numpy(), *want, what=f"range {structure} sample")
+    ix.close()

@@ -54,3 +54,24 @@ def test_noalloc_rejects_batches_beyond_its_scratch():
     st = _noalloc(lib, pts, qs, 128, float("inf"), idx, dist)  # 8193 * 128 > 1,048,576
     assert st == _lib.ERR_UNSUPPORTED
     assert b"16 MiB" in lib.knn_last_error()
+
+
+def test_noalloc_leaves_free_device_memory_unchanged():
+    """After a first call (which may let the runtime size its per-thread stack pool for the
+    kernel), a further call changes the device's free memory by nothing: the entry point itself
+    allocates nothing."""
+    import torch
+    from cudaexactknn_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(17)
+    pts = torch.from_numpy(rng.random((50000, 8), dtype=np.float32)).cuda()
+    qs = torch.from_numpy(rng.random((2000, 8), dtype=np.float32)).cuda()
+    idx = torch.empty((2000, 64), dtype=torch.int32, device="cuda")
+    dist = torch.empty((2000, 64), dtype=torch.float32, device="cuda")
+    _lib.check(_noalloc(lib, pts, qs, 64, float("inf"), idx, dist))
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    _lib.check(_noalloc(lib, pts, qs, 64, float("inf"), idx, dist))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
