@@ -187,8 +187,11 @@ int batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, vo
         c.plan.block = 128;
         if (flags & KNN_QF_AUTOTUNE) {
             const auto& it = items[largest];
-            const knn::QueryArgs a = item_args(it);
+            knn::QueryArgs a = item_args(it);
             if ((rc = knn::tune_plan(it.index, a, s, &c.plan)) != KNN_OK) break;
+            // The filter-or-tree choice below times both forms on the set's first 8,192 queries
+            // (a whole set of 32-dimensional uniform points takes seconds per tree search).
+            a.count = std::min<uint32_t>(a.count, 8192u);
             c.plan.heap = c.plan.sh_nn = c.plan.sh_stack = false;  // the batch kernels keep tracker and stack in registers
             // dims >= 16: the tensor-core filter instead, when it beats the tuned search on the
             // class's largest set.

@@ -203,6 +203,60 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
     KNN_TRY_CUDA(cudaEventCreate(&e1));
     int rc = KNN_OK;
     uint32_t n_tried = 0;
+    // Sample size from a first run of the default plan on 1,024 queries: about 8 ms of search per
+    // candidate run (at least 1,024 queries), so that slow workloads (trees in 32 dimensions that
+    // visit most of their nodes) tune in seconds.
+    if (t.count > 1024) {
+        knn::QueryArgs probe = t;
+        probe.count = 1024;
+        knn::QueryPlan base;
+        base.block = 128;
+        float ms = 0.0f;
+        int prc = cudaEventRecord(e0, s) == cudaSuccess ? KNN_OK : KNN_ERR_CUDA;
+        if (prc == KNN_OK) prc = learned ? seeded_query(ix, probe, base, s) : dispatch(ix, probe, base, s);
+        if (prc == KNN_OK && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                              cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+            prc = knn::fail(KNN_ERR_CUDA, "autotune: timing the sample");
+        if (prc != KNN_OK) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return prc;
+        }
+        const double per_query = std::max(1e-6, static_cast<double>(ms) / 1024.0);
+        const uint32_t fit = static_cast<uint32_t>(std::min(1e9, 8.0 / per_query));
+        t.count = std::max(1024u, std::min(t.count, fit & ~127u));
+    }
+    // k-d trees: the batch's first queries are a sparser set than the batch (fewer queries per
+    // region of space), which misjudges the warp-group search, whose cost depends on how close a
+    // warp's queries are.  The sample is instead four runs of the batch's locality order (at its
+    // quarters), gathered into scratch: it has the batch's density.  Its rows are written to the
+    // first rows of the caller's result buffers, which the real pass then overwrites.
+    if (ix->structure == KNN_KD_TREE && a.count > t.count && !a.order && !a.count_dev) do {
+        const uint32_t* order = nullptr;
+        if ((rc = knn::kd_order(ix, a, s, &order)) != KNN_OK) break;
+        if (order) {
+            const size_t m = t.count;
+            if ((rc = ix->tune_ws.reserve(knn::carve_bytes({m * ix->dims * 4, m * 4}))) != KNN_OK) break;
+            knn::Carver c(ix->tune_ws.ptr);
+            float* sq = c.take<float>(m * ix->dims);
+            float* sr = c.take<float>(m);
+            const uint32_t run = t.count / 4;
+            for (uint32_t r = 0; r < 4 && rc == KNN_OK; ++r) {
+                const uint32_t first = static_cast<uint32_t>((static_cast<uint64_t>(a.count) * (2 * r + 1)) / 8);
+                const uint32_t at = std::min(first, a.count - run);
+                rc = knn::gather_rows(a.queries, a.radii, order + at, run, ix->dims,
+                                      sq + static_cast<size_t>(r) * run * ix->dims, sr + static_cast<size_t>(r) * run, s);
+            }
+            t.count = 4 * run;
+            t.queries = sq;
+            t.radii = a.radii ? sr : nullptr;
+        }
+    } while (false);
+    if (rc != KNN_OK) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return rc;
+    }
     auto time_plan = [&](const knn::QueryPlan& p, float* ms) -> int {
         float best = 1e30f;
         for (int rep = 0; rep < 3; ++rep) {
@@ -235,8 +289,9 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
     do {
         // The tensor-core filter, for dims >= 16 (the form it is built for), on any structure.
         const bool try_tc = allow_tc && ix->dims >= 16 && knn::tc_supported(ix->dims, a.k);
-        if (ix->structure == KNN_KD_TREE && ix->dp <= 16 && a.k <= 32) {
-            // The warp-group search, seeded by the radius model or by each query's own subtree.
+        if (learned && ix->structure == KNN_KD_TREE && ix->dp <= 16 && a.k <= 32) {
+            // The warp-group search, seeded by the radius model (seeds from each query's own
+            // subtree are too loose to pay).
             for (uint32_t leaf : {4u, 8u, 16u, 32u}) {
                 knn::QueryPlan p;
                 p.block = 128;
@@ -495,55 +550,31 @@ int knn_query_host(knn_index* index, const float* h_queries, uint32_t count, flo
     float* dq = c.take<float>(static_cast<size_t>(count) * index->dims);
     int32_t* di = c.take<int32_t>(static_cast<size_t>(count) * k);
     float* dd = c.take<float>(static_cast<size_t>(count) * k);
-    // Chunks of at least 131,072 queries (smaller ones would leave the GPU part idle), at most 8.
-    constexpr uint32_t kMinChunk = 131072;
-    const uint32_t chunks = std::min<uint32_t>(knn::HostIo::kMaxChunks, std::max(1u, count / kMinChunk));
-    if (chunks == 1) {
-        KNN_TRY_CUDA(cudaMemcpyAsync(dq, h_queries, qb, cudaMemcpyHostToDevice, s));
-        knn::QueryArgs a{dq, count, max_distance2, nullptr, k, di, dd, nullptr};
-        KNN_TRY(run_query(index, a, opts, s));
-        KNN_TRY_CUDA(cudaMemcpyAsync(h_indexes, di, rb, cudaMemcpyDeviceToHost, s));
-        KNN_TRY_CUDA(cudaMemcpyAsync(h_distances, dd, rb, cudaMemcpyDeviceToHost, s));
-        KNN_TRY_CUDA(cudaStreamSynchronize(s));
-        return KNN_OK;
-    }
-    // Copy-in, search and copy-out overlap across chunks: the copy streams start after the work
-    // already queued on the caller's stream (which may still read the staging buffers), chunk i's
-    // search waits for its copy-in, its copy-out for its search, and the caller's stream ends
-    // after the last copy-out.
+    KNN_TRY_CUDA(cudaMemcpyAsync(dq, h_queries, qb, cudaMemcpyHostToDevice, s));
+    knn::QueryArgs a{dq, count, max_distance2, nullptr, k, di, dd, nullptr};
+    KNN_TRY(run_query(index, a, opts, s));
+    // The rows go out in pieces on the index's copy streams at once (several copy engines), each
+    // piece after the search; the caller's stream then waits for every piece.
     knn::HostIo& io = index->host_io;
     KNN_TRY(io.ensure());
     KNN_TRY_CUDA(cudaEventRecord(io.start, s));
-    KNN_TRY_CUDA(cudaStreamWaitEvent(io.in, io.start, 0));
-    KNN_TRY_CUDA(cudaStreamWaitEvent(io.out, io.start, 0));
-    const uint32_t per = (count + chunks - 1) / chunks;
-    for (uint32_t i = 0; i < chunks; ++i) {
-        const size_t first = static_cast<size_t>(i) * per, n = std::min<size_t>(per, count - first);
-        KNN_TRY_CUDA(cudaMemcpyAsync(dq + first * index->dims, h_queries + first * index->dims, n * qrow,
-                                     cudaMemcpyHostToDevice, io.in));
-        KNN_TRY_CUDA(cudaEventRecord(io.copied[i], io.in));
+    constexpr int P = knn::HostIo::kParts;
+    const uint32_t per = (count + P / 2 - 1) / (P / 2);  // rows per piece: two pieces per array
+    for (int i = 0; i < P; ++i) {
+        const uint32_t first = (i / 2) * per;
+        if (first >= count) continue;
+        const size_t rows = std::min<uint32_t>(per, count - first);
+        KNN_TRY_CUDA(cudaStreamWaitEvent(io.part[i], io.start, 0));
+        const size_t off = static_cast<size_t>(first) * k;
+        if (i % 2 == 0)
+            KNN_TRY_CUDA(cudaMemcpyAsync(h_indexes + off, di + off, rows * rrow, cudaMemcpyDeviceToHost, io.part[i]));
+        else
+            KNN_TRY_CUDA(cudaMemcpyAsync(h_distances + off, dd + off, rows * rrow, cudaMemcpyDeviceToHost, io.part[i]));
+        KNN_TRY_CUDA(cudaEventRecord(io.done[i], io.part[i]));
+        KNN_TRY_CUDA(cudaStreamWaitEvent(s, io.done[i], 0));
     }
-    int rc = KNN_OK;
-    for (uint32_t i = 0; i < chunks && rc == KNN_OK; ++i) {
-        const size_t first = static_cast<size_t>(i) * per, n = std::min<size_t>(per, count - first);
-        KNN_TRY_CUDA(cudaStreamWaitEvent(s, io.copied[i], 0));
-        knn::QueryArgs a{dq + first * index->dims, static_cast<uint32_t>(n), max_distance2, nullptr, k,
-                         di + first * k, dd + first * k, nullptr};
-        rc = run_query(index, a, opts, s);
-        if (rc != KNN_OK) break;
-        KNN_TRY_CUDA(cudaEventRecord(io.answered[i], s));
-        KNN_TRY_CUDA(cudaStreamWaitEvent(io.out, io.answered[i], 0));
-        KNN_TRY_CUDA(cudaMemcpyAsync(h_indexes + first * k, di + first * k, n * rrow, cudaMemcpyDeviceToHost, io.out));
-        KNN_TRY_CUDA(cudaMemcpyAsync(h_distances + first * k, dd + first * k, n * rrow, cudaMemcpyDeviceToHost,
-                                     io.out));
-    }
-    // Whatever happened, the caller's stream must not run ahead of the copies still in flight.
-    KNN_TRY_CUDA(cudaEventRecord(io.finish, io.out));
-    KNN_TRY_CUDA(cudaStreamWaitEvent(s, io.finish, 0));
-    KNN_TRY_CUDA(cudaEventRecord(io.finish, io.in));
-    KNN_TRY_CUDA(cudaStreamWaitEvent(s, io.finish, 0));
     KNN_TRY_CUDA(cudaStreamSynchronize(s));
-    return rc;
+    return KNN_OK;
 }
 
 int knn_query_stats(knn_index* index, const float* d_queries, uint32_t count, float max_distance2, uint32_t k,

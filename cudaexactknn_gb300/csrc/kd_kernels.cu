@@ -334,8 +334,9 @@ int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStrea
 // bound is a rigorous lower bound on the float distance of every point inside (below).
 constexpr uint32_t kGroupWarps = 4;
 constexpr uint32_t kGroupList = 64;   // bucket entries collected before they are scanned
-constexpr uint32_t kGroupStack = 40;  // node stack (the walk holds at most depth + 1 entries)
-constexpr uint32_t kGroupRounds = 4;  // radius growth rounds before the per-thread fallback
+constexpr uint32_t kGroupFan = 3;     // levels the walk descends per step (up to 8 boxes tested at once)
+constexpr uint32_t kGroupStack = 96;  // node stack (at most 7 net entries per step, 11 steps deep)
+constexpr uint32_t kGroupRounds = 6;  // radius growth rounds before the per-thread fallback
 
 __host__ __device__ constexpr uint32_t group_cap(int kmax) { return kmax <= 8 ? 32u : (kmax <= 16 ? 64u : 96u); }
 __host__ __device__ constexpr int box_qs(int dp) { return dp < 4 ? 4 : dp; }
@@ -459,8 +460,12 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
 #pragma unroll
                 for (int d = 0; d < DP; ++d) qq[d] = sm.qv[ql][d];
                 const float rq = sm.rad[ql];
-                const SlotRange sr = subtree_slots(static_cast<uint32_t>(ent >> 32), stop, p.node_depth, p.node_count,
-                                                   p.leaf_slots);
+                const uint32_t bucket = static_cast<uint32_t>(ent >> 32);
+                if (heap_depth(bucket) != stop) {  // cannot happen (the walk lists buckets only); recorded
+                    stack_error = true;
+                    continue;
+                }
+                const SlotRange sr = subtree_slots(bucket, stop, p.node_depth, p.node_count, p.leaf_slots);
                 const float* slot = p.leaf + sr.first * p.leaf_stride;
 #pragma unroll 4
                 for (uint32_t s = 0; s < bucket_slots; ++s, slot += p.leaf_stride) {
@@ -496,33 +501,44 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
         while (top) {
             __syncwarp();
             const uint32_t node = sm.stack[--top];
-            const uint32_t l = 2 * node + 1;
-            const float bl = box_bound<DP>(q, gp.box + static_cast<size_t>(l) * gp.box_stride);
-            const float br = box_bound<DP>(q, gp.box + static_cast<size_t>(l + 1) * gp.box_stride);
-            const uint32_t ml = __ballot_sync(FULL, bl <= rl);
-            const uint32_t mr = __ballot_sync(FULL, br <= rl);
+            // The node's descendants `levels` below (up to 8, contiguous in the heap order) are
+            // tested at once: their box loads are independent, so they overlap in flight.
+            const uint32_t levels = min(kGroupFan, stop - heap_depth(node));
+            const uint32_t fan = 1u << levels;
+            const uint32_t first = ((node + 1) << levels) - 1;
+            uint32_t want[1u << kGroupFan];
+#pragma unroll
+            for (uint32_t j = 0; j < (1u << kGroupFan); ++j) {
+                // (j < fan first: with an unbounded radius an infinite bound is still "within".)
+                const bool in = j < fan && box_bound<DP>(q, gp.box + static_cast<size_t>(first + j) * gp.box_stride) <= rl;
+                want[j] = __ballot_sync(FULL, in);
+            }
             ++nodes;
-            if (heap_depth(node) + 1 == stop) {
-                if (lane == 0) {
-                    if (ml) sm.list[nlist] = (static_cast<uint64_t>(l) << 32) | ml;
-                    if (mr) sm.list[nlist + (ml ? 1 : 0)] = (static_cast<uint64_t>(l + 1) << 32) | mr;
+            if (heap_depth(node) + levels == stop) {
+#pragma unroll
+                for (uint32_t j = 0; j < (1u << kGroupFan); ++j) {
+                    if (want[j]) {
+                        if (lane == 0) sm.list[nlist] = (static_cast<uint64_t>(first + j) << 32) | want[j];
+                        ++nlist;
+                    }
                 }
-                nlist += (ml ? 1u : 0u) + (mr ? 1u : 0u);
-                if (nlist + 2 > kGroupList) {
+                if (nlist + (1u << kGroupFan) > kGroupList) {
                     __syncwarp();
                     scan(nlist);
                     nlist = 0;
                 }
             } else {
-                if (top + 2 > kGroupStack) {  // cannot happen (at most one entry per level); recorded
+                if (top + (1u << kGroupFan) > kGroupStack) {  // cannot happen (see kGroupStack); recorded
                     stack_error = true;
                     continue;
                 }
-                if (lane == 0) {
-                    if (mr) sm.stack[top] = l + 1;
-                    if (ml) sm.stack[top + (mr ? 1 : 0)] = l;
+#pragma unroll
+                for (uint32_t j = (1u << kGroupFan); j-- > 0;) {
+                    if (want[j]) {
+                        if (lane == 0) sm.stack[top] = first + j;
+                        ++top;
+                    }
                 }
-                top += (ml ? 1u : 0u) + (mr ? 1u : 0u);
             }
         }
         if (nlist) {
@@ -553,7 +569,12 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
                 if (p.counters) atomicAdd(&p.counters->fallback, 1ull);
                 pending = false;
             } else {
-                r = fminf(R, fmaxf(r * 4.0f, 1e-30f));
+                // Fewer than k within r: grow r^2 by the volume ratio k points need at the density
+                // seen, (1.5 k / c)^(2 / dims), between 1.25 and 16.
+                const float ce = fmaxf(static_cast<float>(c), 0.5f);
+                const float g = fminf(fmaxf(exp2f(log2f(1.5f * static_cast<float>(p.k) / ce) * (2.0f / p.dims)), 1.25f),
+                                      16.0f);
+                r = fminf(R, fmaxf(r * g, 1e-30f));
             }
         }
         __syncwarp();

@@ -235,34 +235,27 @@ struct StreamOrder {
     }
 };
 
-// knn_query_host's copy pipeline: queries are answered in chunks; chunk i+1's queries are copied
-// in on `in` while chunk i is searched on the caller's stream and chunk i-1's rows are copied out
-// on `out`.
+// knn_query_host's copy streams: the result rows (by far the larger transfer) are copied out in
+// kParts pieces on as many streams at once, so that several copy engines move them.
 struct HostIo {
-    static constexpr int kMaxChunks = 8;
-    cudaStream_t in = nullptr, out = nullptr;
-    cudaEvent_t start = nullptr, finish = nullptr;
-    cudaEvent_t copied[kMaxChunks] = {}, answered[kMaxChunks] = {};
+    static constexpr int kParts = 4;
+    cudaStream_t part[kParts] = {};
+    cudaEvent_t start = nullptr;
+    cudaEvent_t done[kParts] = {};
     ~HostIo() {
-        for (cudaEvent_t e : {start, finish})
-            if (e) cudaEventDestroy(e);
-        for (int i = 0; i < kMaxChunks; ++i) {
-            if (copied[i]) cudaEventDestroy(copied[i]);
-            if (answered[i]) cudaEventDestroy(answered[i]);
+        if (start) cudaEventDestroy(start);
+        for (int i = 0; i < kParts; ++i) {
+            if (done[i]) cudaEventDestroy(done[i]);
+            if (part[i]) cudaStreamDestroy(part[i]);
         }
-        if (in) cudaStreamDestroy(in);
-        if (out) cudaStreamDestroy(out);
     }
     int ensure() {
-        if (in) return KNN_OK;
-        KNN_TRY_CUDA(cudaStreamCreateWithFlags(&in, cudaStreamNonBlocking));
-        KNN_TRY_CUDA(cudaStreamCreateWithFlags(&out, cudaStreamNonBlocking));
-        KNN_TRY_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
-        KNN_TRY_CUDA(cudaEventCreateWithFlags(&finish, cudaEventDisableTiming));
-        for (int i = 0; i < kMaxChunks; ++i) {
-            KNN_TRY_CUDA(cudaEventCreateWithFlags(&copied[i], cudaEventDisableTiming));
-            KNN_TRY_CUDA(cudaEventCreateWithFlags(&answered[i], cudaEventDisableTiming));
+        if (start) return KNN_OK;
+        for (int i = 0; i < kParts; ++i) {
+            KNN_TRY_CUDA(cudaStreamCreateWithFlags(&part[i], cudaStreamNonBlocking));
+            KNN_TRY_CUDA(cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming));
         }
+        KNN_TRY_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
         return KNN_OK;
     }
 };
@@ -343,6 +336,7 @@ struct knn_index {
     bool has_model = false;
     uint32_t model_k = 0;     // k the model was trained for
     knn::DevBuf seed_ws;      // seeded radii, fallback list and count
+    knn::DevBuf tune_ws;      // the autotuner's gathered sample (queries, radii)
 
     // Autotuned plans, one per k class (8, 16, 32, 64, 128) and learned-radius on/off.
     struct Tuned {
@@ -361,6 +355,10 @@ namespace knn {
 size_t radix_sort_temp_bytes(uint32_t n);
 int radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt,
                      uint32_t n, int key_bits, void* temp, cudaStream_t s, bool* in_alt);
+
+// dst[i] = rows idx[i] of src ([*][dims] floats); dst_radii[i] = src_radii[idx[i]] when src_radii.
+int gather_rows(const float* src, const float* src_radii, const uint32_t* idx, uint32_t count, uint32_t dims,
+                float* dst, float* dst_radii, cudaStream_t s);
 
 // Exclusive prefix sum of per-block counts: counts[rows][cols] row-major -> out, each row
 // scanned independently (one thread block per row).

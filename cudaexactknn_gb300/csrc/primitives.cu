@@ -160,7 +160,29 @@ __global__ void fill_rows_kernel(uint32_t count, uint32_t k, float max_d2, const
     dist[i] = radii ? radii[i / k] : max_d2;
 }
 
+// dst[i] = src row idx[i] (rows of `dims` floats), and the per-row radius when given.
+__global__ void gather_rows_kernel(const float* __restrict__ src, const float* __restrict__ src_r,
+                                   const uint32_t* __restrict__ idx, uint32_t count, uint32_t dims,
+                                   float* __restrict__ dst, float* __restrict__ dst_r) {
+    const uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= static_cast<uint64_t>(count) * dims) return;
+    const uint32_t i = static_cast<uint32_t>(e / dims), d = static_cast<uint32_t>(e % dims);
+    const uint32_t j = idx[i];
+    dst[e] = src[static_cast<size_t>(j) * dims + d];
+    if (src_r && d == 0) dst_r[i] = src_r[j];
+}
+
 }  // namespace
+
+int gather_rows(const float* src, const float* src_radii, const uint32_t* idx, uint32_t count, uint32_t dims,
+                float* dst, float* dst_radii, cudaStream_t s) {
+    if (!count) return KNN_OK;
+    const uint64_t total = static_cast<uint64_t>(count) * dims;
+    gather_rows_kernel<<<static_cast<uint32_t>((total + 255) / 256), 256, 0, s>>>(src, src_radii, idx, count, dims,
+                                                                                dst, dst_radii);
+    KNN_LAUNCHED();
+    return KNN_OK;
+}
 
 size_t radix_sort_temp_bytes(uint32_t n) {
     const size_t nblocks = (static_cast<size_t>(n) + kSortTile - 1) / kSortTile;

@@ -196,12 +196,12 @@ KNN_API int knn_query_radii(knn_index* index, const float* d_queries, uint32_t c
                     const float* d_max_distance2, uint32_t k, int32_t* d_indexes,
                     float* d_distances, const knn_query_opts* opts, void* stream);
 
-/* As knn_query with HOST buffers, and synchronises.  Batches of at least 262,144 queries are
- * answered in up to 8 chunks (>= 131,072 queries each) whose copies overlap the search: chunk i+1
- * is copied in on one of the index's copy streams while chunk i is searched on `stream` and chunk
- * i-1's rows are copied out on the other (one cudaMemcpyAsync per chunk and array).  Replaces the
- * reference's copy, batchKnn and device-wide synchronisation (src/KdTreeGpu.cuh:394-410,
- * src/BruteForceGpu.cuh:75-83).  Pinned host memory gives full-speed, asynchronous copies. */
+/* As knn_query with HOST buffers, and synchronises: the queries are copied in on `stream`, the
+ * search runs there, and the result rows go out in four pieces on four copy streams of the index
+ * at once (one cudaMemcpyAsync each), so that several copy engines share the larger transfer.
+ * Replaces the reference's copy, batchKnn and device-wide synchronisation
+ * (src/KdTreeGpu.cuh:394-410, src/BruteForceGpu.cuh:75-83).  Pinned host memory gives
+ * full-speed, asynchronous copies. */
 KNN_API int knn_query_host(knn_index* index, const float* h_queries, uint32_t count,
                    float max_distance2, uint32_t k, int32_t* h_indexes, float* h_distances,
                    const knn_query_opts* opts, void* stream);

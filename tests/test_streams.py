@@ -1,6 +1,7 @@
 """Streams and host buffers: different indexes on different non-default streams run at the same
 time, queries on one index from two streams are ordered on the device (they share its scratch),
-and knn_query_host's chunked copy pipeline returns what the device-buffer call returns."""
+and knn_query_host (result rows copied out in pieces on several streams) returns what the
+device-buffer call returns."""
 
 import numpy as np
 import pytest
@@ -75,8 +76,8 @@ def test_one_index_from_two_streams(structure):
 
 @pytest.mark.parametrize("learned", [False, True])
 def test_host_pipeline_matches_device_call(learned):
-    """600,000 queries: knn_query_host answers them in four chunks whose copies overlap the
-    search; rows equal knn_query on device buffers, bit for bit, and a sample equals the oracle."""
+    """600,000 queries through knn_query_host: rows equal knn_query on device buffers, bit for
+    bit, call after call, and a sample equals the oracle."""
     import torch
     from cudaexactknn_gb300 import _lib
     rng = np.random.default_rng(8)
