@@ -187,24 +187,40 @@ int batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, vo
         c.plan.block = 128;
         if (flags & KNN_QF_AUTOTUNE) {
             const auto& it = items[largest];
-            knn::QueryArgs a = item_args(it);
-            if ((rc = knn::tune_plan(it.index, a, s, &c.plan)) != KNN_OK) break;
-            // The filter-or-tree choice below times both forms on the set's first 8,192 queries
-            // (a whole set of 32-dimensional uniform points takes seconds per tree search).
-            a.count = std::min<uint32_t>(a.count, 8192u);
-            c.plan.heap = c.plan.sh_nn = c.plan.sh_stack = false;  // the batch kernels keep tracker and stack in registers
-            // dims >= 16: the tensor-core filter instead, when it beats the tuned search on the
-            // class's largest set.
+            const knn::QueryArgs a = item_args(it);
+            // dims >= 16: the tensor-core filter instead of the class's tree search when it is
+            // faster per query on the class's largest set.  Both are first timed on a sample (the
+            // filter on 8,192 queries, the tree's default search on 1,024: a whole set of
+            // 32-dimensional uniform points takes seconds per tree search); a filter four times
+            // faster than that settles it, otherwise the tree is autotuned and compared again.
             bool tc_ok = it.index->dims >= 16;
             for (uint32_t i : c.items) tc_ok = tc_ok && knn::tc_supported(items[i].index->dims, items[i].k);
+            float tc_per_q = 0.0f;
             if (tc_ok) {
                 knn::QueryPlan tp;
                 tp.bf16 = true;
+                knn::QueryArgs at = a, ad = a;
+                at.count = std::min<uint32_t>(a.count, 8192u);
+                ad.count = std::min<uint32_t>(a.count, 1024u);
                 float t_tc = 0.0f, t_tree = 0.0f;
-                if ((rc = time_query([&] { return knn::bf_tc_query(it.index, a, tp, s); }, s, &t_tc)) != KNN_OK) break;
-                if ((rc = time_query([&] { return knn::query_structure(it.index, a, c.plan, s); }, s, &t_tree)) != KNN_OK)
+                if ((rc = time_query([&] { return knn::bf_tc_query(it.index, at, tp, s); }, s, &t_tc)) != KNN_OK) break;
+                if ((rc = time_query([&] { return knn::query_structure(it.index, ad, c.plan, s); }, s, &t_tree)) != KNN_OK)
                     break;
-                c.tc = t_tc < t_tree;
+                tc_per_q = t_tc / at.count;
+                c.tc = 4.0f * tc_per_q < t_tree / ad.count;
+            }
+            if (!c.tc) {
+                if ((rc = knn::tune_plan(it.index, a, s, &c.plan)) != KNN_OK) break;
+                c.plan.heap = c.plan.sh_nn = c.plan.sh_stack = false;  // the batch kernels keep tracker and stack in registers
+                if (tc_ok) {
+                    knn::QueryArgs at = a;
+                    at.count = std::min<uint32_t>(a.count, 8192u);
+                    float t_tree = 0.0f;
+                    if ((rc = time_query([&] { return knn::query_structure(it.index, at, c.plan, s); }, s, &t_tree)) !=
+                        KNN_OK)
+                        break;
+                    c.tc = tc_per_q < t_tree / at.count;
+                }
             }
         }
         if (c.tc) {

@@ -134,7 +134,9 @@ int dispatch(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& plan,
 // Learned radius: seed each query's radius from the model and search.  Queries that found fewer
 // than k points inside a seed below the caller's radius are searched again with the radius
 // grown 16x (squared distance), twice, and then with the caller's radius, which makes every
-// answer exact.  Retry lists keep the locality order of the batch.
+// answer exact.  Retry lists keep the locality order of the batch.  (Growing each query by the
+// density it saw, (1.5 k / c)^(2/D), was tried on the mixture workload and was slower: queries
+// that miss by a little take one more round, and each round is a launch over a scattered list.)
 constexpr int kSeedRounds = 3;
 constexpr float kSeedGrowth = 16.0f;
 
@@ -257,8 +259,11 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
         cudaEventDestroy(e1);
         return rc;
     }
+    knn::QueryPlan best;
+    best.block = 128;
+    float best_t = 1e30f;
     auto time_plan = [&](const knn::QueryPlan& p, float* ms) -> int {
-        float best = 1e30f;
+        float best_rep = 1e30f;
         for (int rep = 0; rep < 3; ++rep) {
             KNN_TRY_CUDA(cudaEventRecord(e0, s));
             KNN_TRY(learned ? seeded_query(ix, t, p, s) : dispatch(ix, t, p, s));
@@ -266,15 +271,18 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
             KNN_TRY_CUDA(cudaEventSynchronize(e1));
             float v = 0.0f;
             KNN_TRY_CUDA(cudaEventElapsedTime(&v, e0, e1));
-            if (rep > 0) best = std::min(best, v);  // the first run warms caches and workspaces
+            if (rep > 0) best_rep = std::min(best_rep, v);  // the first run warms caches and workspaces
+            // A candidate whose first run already takes 4x the best plan's time cannot win: its
+            // warm runs are skipped (in 32-dimensional trees a run can take seconds).
+            if (rep == 0 && v > 4.0f * best_t) {
+                best_rep = v;
+                break;
+            }
         }
-        *ms = best;
+        *ms = best_rep;
         ++n_tried;
         return KNN_OK;
     };
-    knn::QueryPlan best;
-    best.block = 128;
-    float best_t = 1e30f;
     auto consider = [&](const knn::QueryPlan& p) -> int {
         float v = 0.0f;
         const int r = time_plan(p, &v);
@@ -301,6 +309,13 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
             }
             if (rc != KNN_OK) break;
         }
+        if (ix->structure != KNN_BRUTE_FORCE && try_tc) {
+            // First, so that slow tree candidates are cut short against its time.
+            knn::QueryPlan p;
+            p.block = 128;
+            p.bf16 = true;
+            if ((rc = consider(p)) != KNN_OK) break;
+        }
         if (ix->structure != KNN_BRUTE_FORCE) {
             for (bool warp : {false, true}) {
                 for (uint32_t leaf : {0u, 4u, 8u, 16u, 32u, 64u}) {
@@ -315,12 +330,6 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
                 if (rc != KNN_OK) break;
             }
             if (rc != KNN_OK) break;
-            if (try_tc) {
-                knn::QueryPlan p;
-                p.block = 128;
-                p.bf16 = true;
-                if ((rc = consider(p)) != KNN_OK) break;
-            }
         } else {
             if ((rc = consider(best)) != KNN_OK) break;
             if (try_tc) {

@@ -343,7 +343,7 @@ __host__ __device__ constexpr int box_qs(int dp) { return dp < 4 ? 4 : dp; }
 
 template <int DP, int KMAX>
 struct GroupWarpSmem {
-    uint64_t buf[group_cap(KMAX)][32];  // candidate keys, slot-major (slot i of lane l at [i][l])
+    uint32_t buf[group_cap(KMAX)][32];  // candidates' leaf slots, slot-major (entry i of lane l at [i][l])
     uint64_t list[kGroupList];          // (bucket node << 32) | lanes
     float qv[32][box_qs(DP)];           // the warp's queries
     float rad[32];                      // radius of each lane this round (-1: none)
@@ -472,8 +472,10 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
                     int32_t id;
                     const float d2 = slot_dist<DP>(qq, slot, &id);
                     if (id >= 0 && d2 <= rq) {
+                        // The slot is kept, not the key: half the shared memory, and the owner lane
+                        // recomputes the same distance from it when it sorts its list.
                         const uint32_t pos = atomicAdd(&sm.cnt[ql], 1u);
-                        if (pos < C) sm.buf[pos][ql] = make_key(d2, id);
+                        if (pos < C) sm.buf[pos][ql] = static_cast<uint32_t>(sr.first) + s;
                     }
                 }
                 ++pairs;
@@ -559,7 +561,11 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
             } else if (c >= p.k || !(r < R)) {
                 Tracker<KMAX, false, false> tr;
                 tr.init(p.k, R, nullptr, 0);
-                for (uint32_t i = 0; i < c; ++i) tr.offer(sm.buf[i][lane]);
+                for (uint32_t i = 0; i < c; ++i) {
+                    int32_t id;
+                    const float d2 = slot_dist<DP>(q, p.leaf + static_cast<size_t>(sm.buf[i][lane]) * p.leaf_stride, &id);
+                    tr.offer(make_key(d2, id));
+                }
                 tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
                 pending = false;
             } else if (round + 1 >= kGroupRounds) {
