@@ -160,8 +160,11 @@ int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& p
     KNN_TRY(knn::model_predict(ix->model.as<float>(), ix->dims, a.queries, a.count, a.max_d2, a.radii, radii,
                                nullptr, s, true));
     // The warp-group k-d search settles or hands on every query itself (no retry rounds).
+    // Its seeds may be widened by a factor exp(widen * margin / 2) that the autotuner picks: a
+    // miss costs the warp another walk, a wider seed only a few more candidates per query.
     if (plan.group && ix->structure == KNN_KD_TREE)
-        return knn::kd_group_query(ix, a, plan, order, radii, list, list_count, s);
+        return knn::kd_group_query(ix, a, plan, order, radii, list, list_count,
+                                   std::exp(0.5f * static_cast<float>(plan.widen) * ix->model_margin), s);
     knn::QueryArgs seeded = a;
     seeded.radii = radii;
     seeded.order = order;
@@ -300,12 +303,16 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
         if (learned && ix->structure == KNN_KD_TREE && ix->dp <= 16 && a.k <= 32) {
             // The warp-group search, seeded by the radius model (seeds from each query's own
             // subtree are too loose to pay).
-            for (uint32_t leaf : {4u, 8u, 16u, 32u}) {
-                knn::QueryPlan p;
-                p.block = 128;
-                p.group = true;
-                p.leaf_scan = leaf;
-                if ((rc = consider(p)) != KNN_OK) break;
+            for (uint32_t leaf : {8u, 16u, 32u}) {
+                for (uint32_t widen : {0u, 1u, 2u}) {
+                    knn::QueryPlan p;
+                    p.block = 128;
+                    p.group = true;
+                    p.leaf_scan = leaf;
+                    p.widen = widen;
+                    if ((rc = consider(p)) != KNN_OK) break;
+                }
+                if (rc != KNN_OK) break;
             }
             if (rc != KNN_OK) break;
         }
@@ -698,6 +705,7 @@ int knn_radius_model_import(knn_index* index, const float* h_params, uint32_t co
     KNN_TRY_CUDA(cudaMemcpy(index->model.ptr, h_params, n * 4, cudaMemcpyHostToDevice));
     index->has_model = true;
     index->model_k = k;
+    index->model_margin = h_params[n - 1];  // the margin is the model's last parameter
     return KNN_OK;
 }
 

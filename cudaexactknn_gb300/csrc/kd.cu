@@ -21,7 +21,7 @@ template <uint32_t DP>
 int kd_order_dp(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
 template <uint32_t DP>
 int kd_group_query_dp(knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, float*, uint32_t*, uint32_t*,
-                      cudaStream_t);
+                      float, cudaStream_t);
 
 namespace {
 
@@ -146,14 +146,14 @@ int kd_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t
 }
 
 int kd_group_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, const uint32_t* order, float* seeds,
-                   uint32_t* fb_list, uint32_t* fb_count, cudaStream_t s) {
+                   uint32_t* fb_list, uint32_t* fb_count, float seed_scale, cudaStream_t s) {
     switch (ix->dp) {
-        case 1: return kd_group_query_dp<1>(ix, a, p, order, seeds, fb_list, fb_count, s);
-        case 2: return kd_group_query_dp<2>(ix, a, p, order, seeds, fb_list, fb_count, s);
-        case 3: return kd_group_query_dp<3>(ix, a, p, order, seeds, fb_list, fb_count, s);
-        case 4: return kd_group_query_dp<4>(ix, a, p, order, seeds, fb_list, fb_count, s);
-        case 8: return kd_group_query_dp<8>(ix, a, p, order, seeds, fb_list, fb_count, s);
-        case 16: return kd_group_query_dp<16>(ix, a, p, order, seeds, fb_list, fb_count, s);
+        case 1: return kd_group_query_dp<1>(ix, a, p, order, seeds, fb_list, fb_count, seed_scale, s);
+        case 2: return kd_group_query_dp<2>(ix, a, p, order, seeds, fb_list, fb_count, seed_scale, s);
+        case 3: return kd_group_query_dp<3>(ix, a, p, order, seeds, fb_list, fb_count, seed_scale, s);
+        case 4: return kd_group_query_dp<4>(ix, a, p, order, seeds, fb_list, fb_count, seed_scale, s);
+        case 8: return kd_group_query_dp<8>(ix, a, p, order, seeds, fb_list, fb_count, seed_scale, s);
+        case 16: return kd_group_query_dp<16>(ix, a, p, order, seeds, fb_list, fb_count, seed_scale, s);
         default: return fail(KNN_ERR_INVALID_ARGUMENT, "group search: dims above 16");
     }
 }

@@ -301,13 +301,13 @@ int kd_order_dp(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_
 
 template <uint32_t DP>
 int kd_group_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order,
-                      float* seeds, uint32_t* fb_list, uint32_t* fb_count, cudaStream_t s);
+                      float* seeds, uint32_t* fb_list, uint32_t* fb_count, float seed_scale, cudaStream_t s);
 
 template <uint32_t DP>
 int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s) {
     const uint32_t* order = a.order;
     if (!order && p.reorder && a.count >= 4096) KNN_TRY(kd_order_dp<DP>(ix, a, s, &order));
-    if (p.group && !a.count_dev) return kd_group_query_dp<DP>(ix, a, p, order, nullptr, nullptr, nullptr, s);
+    if (p.group && !a.count_dev) return kd_group_query_dp<DP>(ix, a, p, order, nullptr, nullptr, nullptr, 1.0f, s);
     switch (k_class(a.k)) {
         case 8: return launch_kd_variant<DP, 8>(ix, a, p, order, s);
         case 16: return launch_kd_variant<DP, 16>(ix, a, p, order, s);
@@ -362,6 +362,7 @@ struct KdGroupParams {
     uint32_t* fb_list;       // queries left to the per-thread search
     uint32_t* fb_count;
     uint32_t box_stride;     // floats per box
+    float seed_scale;        // seeds are multiplied by this (capped by the caller's radius)
 };
 
 // Lower bound on the float dist2 from q to any point of the box (lo, hi): per dimension the gap
@@ -426,7 +427,7 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
 #pragma unroll
     for (int d = 0; d < QS; ++d) sm.qv[lane][d] = d < DP ? q[d] : 0.0f;
     const float R = active ? (p.radii ? p.radii[qi] : p.max_d2) : -1.0f;
-    float r = active ? gp.seeds[qi] : -1.0f;
+    float r = active ? gp.seeds[qi] * gp.seed_scale : -1.0f;
     if (!(r <= R)) r = R;  // a seed above the caller's radius (or NaN) starts at the caller's
     bool pending = active;
     const uint32_t stop = p.stop_depth;
@@ -586,7 +587,7 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
         __syncwarp();
     }
     if (p.counters) {
-        // nodes: popped nodes (each tests its two children); leaves: (bucket, query) pairs.
+        // nodes: walk steps (each tests up to 8 descendants); leaves: (bucket, query) pairs.
         if (lane == 0) {
             atomicAdd(&p.counters->nodes, static_cast<unsigned long long>(nodes));
             if (stack_error) atomicExch(&p.counters->error, 1);
@@ -703,7 +704,8 @@ int kd_box_build_dp(knn_index* ix, cudaStream_t s) {
 
 template <int DP, int KMAX>
 static int launch_kd_group(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order,
-                           float* seeds, bool self_seed, uint32_t* fb_list, uint32_t* fb_count, cudaStream_t s) {
+                           float* seeds, bool self_seed, uint32_t* fb_list, uint32_t* fb_count, float seed_scale,
+                           cudaStream_t s) {
     KdGroupParams gp{};
     KdParams& p = gp.p;
     p.split = ix->split.as<float>();
@@ -728,6 +730,7 @@ static int launch_kd_group(knn_index* ix, const QueryArgs& a, const QueryPlan& p
     gp.box = ix->kd_box.as<float>();
     gp.box_stride = ix->kd_box_stride;
     gp.seeds = seeds;
+    gp.seed_scale = seed_scale;
     gp.fb_list = fb_list;
     gp.fb_count = fb_count;
     KNN_TRY_CUDA(cudaMemsetAsync(fb_count, 0, sizeof(uint32_t), s));
@@ -760,7 +763,7 @@ static int launch_kd_group(knn_index* ix, const QueryArgs& a, const QueryPlan& p
 // (seeds when self-seeded, the fallback list) comes from the index workspace after the order.
 template <uint32_t DP>
 int kd_group_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order,
-                      float* seeds, uint32_t* fb_list, uint32_t* fb_count, cudaStream_t s) {
+                      float* seeds, uint32_t* fb_list, uint32_t* fb_count, float seed_scale, cudaStream_t s) {
     if constexpr (DP > 16) {
         return fail(KNN_ERR_INVALID_ARGUMENT, "group search: dims above 16");
     } else {
@@ -779,16 +782,16 @@ int kd_group_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, 
             fb_count = c.take<uint32_t>(1);
         }
         switch (k_class(a.k)) {
-            case 8: return launch_kd_group<DP, 8>(ix, a, plan, order, seeds, self_seed, fb_list, fb_count, s);
-            case 16: return launch_kd_group<DP, 16>(ix, a, plan, order, seeds, self_seed, fb_list, fb_count, s);
-            default: return launch_kd_group<DP, 32>(ix, a, plan, order, seeds, self_seed, fb_list, fb_count, s);
+            case 8: return launch_kd_group<DP, 8>(ix, a, plan, order, seeds, self_seed, fb_list, fb_count, seed_scale, s);
+            case 16: return launch_kd_group<DP, 16>(ix, a, plan, order, seeds, self_seed, fb_list, fb_count, seed_scale, s);
+            default: return launch_kd_group<DP, 32>(ix, a, plan, order, seeds, self_seed, fb_list, fb_count, seed_scale, s);
         }
     }
 }
 
 template int kd_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
 template int kd_group_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, float*,
-                                        uint32_t*, uint32_t*, cudaStream_t);
+                                        uint32_t*, uint32_t*, float, cudaStream_t);
 template int kd_order_dp<KNN_DP>(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
 
 

@@ -162,6 +162,7 @@ struct QueryPlan {
     bool timing = false;     // record events around the main search kernel
     bool warp = false;       // trees: warp-coherent traversal instead of one search per thread
     bool group = false;      // k-d tree: warp-group search from per-query radii (traversal 2)
+    uint32_t widen = 0;      // group search: learned seeds x exp(widen * margin / 2) (fewer retries)
     bool bf16 = false;       // brute force: BF16 tensor-core filter + FP32 rescoring
     uint32_t tc_cap = 0;     // candidates kept per query by the filter (0 = default)
     uint32_t leaf_scan = 0;  // 0 = tree leaves
@@ -335,6 +336,7 @@ struct knn_index {
     knn::DevBuf model;
     bool has_model = false;
     uint32_t model_k = 0;     // k the model was trained for
+    float model_margin = 0.0f;  // the model's margin (log squared distance), kept on the host
     knn::DevBuf seed_ws;      // seeded radii, fallback list and count
     knn::DevBuf tune_ws;      // the autotuner's gathered sample (queries, radii)
 
@@ -414,7 +416,7 @@ int kd_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t
 // Warp-group k-d search from per-query seed radii (kd_kernels.cu); queries it cannot settle go to
 // fb_list / fb_count and are answered by the per-thread search in the same call.
 int kd_group_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, const uint32_t* order, float* seeds,
-                   uint32_t* fb_list, uint32_t* fb_count, cudaStream_t s);
+                   uint32_t* fb_list, uint32_t* fb_count, float seed_scale, cudaStream_t s);
 int ball_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 
 // Rows of unfilled results (index -1, distance = radius) for an empty point set.

@@ -722,6 +722,7 @@ int model_train(knn_index* ix, const float* d_samples, uint32_t count, uint32_t 
     KNN_TRY_CUDA(cudaEventSynchronize(e1));
     ix->has_model = true;
     ix->model_k = k;
+    ix->model_margin = margin;
     if (rep) {
         std::memset(rep, 0, sizeof(*rep));
         KNN_TRY_CUDA(cudaEventElapsedTime(&rep->train_ms, e0, e1));

@@ -207,6 +207,11 @@ int knn_index_deserialize(const void* host_buf, size_t size, void* stream, knn_i
     }
     ix->has_model = h.has_model != 0;
     ix->model_k = h.model_k;
+    if (ix->has_model) {  // the model's margin is its last parameter (at the end of the blob)
+        float m = 0.0f;
+        std::memcpy(&m, in + size - sizeof(float), sizeof(float));
+        ix->model_margin = m;
+    }
     ix->device_bytes = h.bytes[0] + h.bytes[1] + h.bytes[2] + h.bytes[3];
     *out = ix;
     return KNN_OK;
