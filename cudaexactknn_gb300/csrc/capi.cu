@@ -200,8 +200,11 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
              float* best_ms, uint32_t* tried, bool allow_tc = true) {
     const knn::Range range("autotune");
     knn::QueryArgs t = a;
-    // Brute force costs n distances per query; a smaller sample keeps tuning short.
-    t.count = std::min<uint32_t>(a.count, ix->structure == KNN_BRUTE_FORCE ? 8192u : 32768u);
+    // Brute force costs n distances per query; a smaller sample keeps tuning short.  k-d trees
+    // take up to 131,072 queries: the warp-group search needs enough warps to fill the GPU before
+    // its time per query means what it will mean on a large batch.
+    t.count = std::min<uint32_t>(a.count, ix->structure == KNN_BRUTE_FORCE ? 8192u
+                                          : ix->structure == KNN_KD_TREE ? 131072u : 32768u);
     t.counters = nullptr;
     cudaEvent_t e0, e1;
     KNN_TRY_CUDA(cudaEventCreate(&e0));
@@ -233,26 +236,22 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
     }
     // k-d trees: the batch's first queries are a sparser set than the batch (fewer queries per
     // region of space), which misjudges the warp-group search, whose cost depends on how close a
-    // warp's queries are.  The sample is instead four runs of the batch's locality order (at its
-    // quarters), gathered into scratch: it has the batch's density.  Its rows are written to the
-    // first rows of the caller's result buffers, which the real pass then overwrites.
+    // warp's queries are.  The sample is instead every s-th run of 32 queries of the batch's
+    // locality order (s = count / sample), gathered into scratch: each run is a warp's group as
+    // the real pass has it, and the runs cover the batch's whole extent.  Its rows are written to
+    // the first rows of the caller's result buffers, which the real pass then overwrites.
     if (ix->structure == KNN_KD_TREE && a.count > t.count && !a.order && !a.count_dev) do {
         const uint32_t* order = nullptr;
         if ((rc = knn::kd_order(ix, a, s, &order)) != KNN_OK) break;
         if (order) {
+            t.count &= ~31u;
+            const uint32_t stride = a.count / t.count;  // >= 1; the last run ends below a.count
             const size_t m = t.count;
             if ((rc = ix->tune_ws.reserve(knn::carve_bytes({m * ix->dims * 4, m * 4}))) != KNN_OK) break;
             knn::Carver c(ix->tune_ws.ptr);
             float* sq = c.take<float>(m * ix->dims);
             float* sr = c.take<float>(m);
-            const uint32_t run = t.count / 4;
-            for (uint32_t r = 0; r < 4 && rc == KNN_OK; ++r) {
-                const uint32_t first = static_cast<uint32_t>((static_cast<uint64_t>(a.count) * (2 * r + 1)) / 8);
-                const uint32_t at = std::min(first, a.count - run);
-                rc = knn::gather_rows(a.queries, a.radii, order + at, run, ix->dims,
-                                      sq + static_cast<size_t>(r) * run * ix->dims, sr + static_cast<size_t>(r) * run, s);
-            }
-            t.count = 4 * run;
+            rc = knn::gather_rows(a.queries, a.radii, order, t.count, ix->dims, stride, sq, sr, s);
             t.queries = sq;
             t.radii = a.radii ? sr : nullptr;
         }

@@ -361,6 +361,7 @@ struct KdGroupParams {
     float* seeds;            // per query radius to start from (<= the caller's); fallback radius on exit
     uint32_t* fb_list;       // queries left to the per-thread search
     uint32_t* fb_count;
+    uint32_t* group_counter; // next group of 32 queries (zero before the launch)
     uint32_t box_stride;     // floats per box
     float seed_scale;        // seeds are multiplied by this (capped by the caller's radius)
 };
@@ -417,174 +418,190 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
     Sm& sm = reinterpret_cast<Sm*>(smem_raw)[threadIdx.x >> 5];
     const KdParams& p = gp.p;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t g = (blockIdx.x * kGroupWarps + (threadIdx.x >> 5)) * 32u;
-    if (g >= p.nq) return;  // whole warp idle; warps never wait on one another
-    const uint32_t t = g + lane;
-    const bool active = t < p.nq;
-    const uint32_t qi = active ? (p.order ? p.order[t] : t) : 0u;
-    float q[DP];
-    load_query<DP>(p.queries, p.dims, qi, q);
-#pragma unroll
-    for (int d = 0; d < QS; ++d) sm.qv[lane][d] = d < DP ? q[d] : 0.0f;
-    const float R = active ? (p.radii ? p.radii[qi] : p.max_d2) : -1.0f;
-    float r = active ? gp.seeds[qi] * gp.seed_scale : -1.0f;
-    if (!(r <= R)) r = R;  // a seed above the caller's radius (or NaN) starts at the caller's
-    bool pending = active;
     const uint32_t stop = p.stop_depth;
     const uint32_t bucket_slots = p.leaf_slots << (p.node_depth - stop);
     uint32_t nodes = 0, pairs = 0;
     bool stack_error = false;
+    // Persistent warps: each takes the next group of 32 queries from a counter until the batch is
+    // done, so that no partial last wave of blocks is left and regions of uneven cost balance.
+    for (;;) {
+        uint32_t grp = 0;
+        if (lane == 0) grp = atomicAdd(gp.group_counter, 1u);
+        const uint32_t g = __shfl_sync(FULL, grp, 0) * 32u;
+        if (g >= p.nq) break;
+        const uint32_t t = g + lane;
+        const bool active = t < p.nq;
+        const uint32_t qi = active ? (p.order ? p.order[t] : t) : 0u;
+        float q[DP];
+        load_query<DP>(p.queries, p.dims, qi, q);
+#pragma unroll
+        for (int d = 0; d < QS; ++d) sm.qv[lane][d] = d < DP ? q[d] : 0.0f;
+        const float R = active ? (p.radii ? p.radii[qi] : p.max_d2) : -1.0f;
+        float r = active ? gp.seeds[qi] * gp.seed_scale : -1.0f;
+        if (!(r <= R)) r = R;  // a seed above the caller's radius (or NaN) starts at the caller's
+        bool pending = active;
 
-    // Scans the collected (bucket, lanes) entries, one (bucket, query) pair per lane at a time.
-    auto scan = [&](uint32_t n) {
-        for (uint32_t base = 0; base < n; base += 32) {
-            const uint32_t e = base + lane;
-            const uint32_t m = e < n ? static_cast<uint32_t>(sm.list[e]) : 0u;
-            uint32_t incl = __popc(m);
+        // Scans the collected (bucket, lanes) entries, one (bucket, query) pair per lane at a time.
+        auto scan = [&](uint32_t n) {
+            for (uint32_t base = 0; base < n; base += 32) {
+                const uint32_t e = base + lane;
+                const uint32_t m = e < n ? static_cast<uint32_t>(sm.list[e]) : 0u;
+                uint32_t incl = __popc(m);
 #pragma unroll
-            for (uint32_t o = 1; o < 32; o <<= 1) {
-                const uint32_t v = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o) incl += v;
-            }
-            const uint32_t total = __shfl_sync(FULL, incl, 31);
-            sm.pre[lane] = incl;
-            __syncwarp();
-            for (uint32_t it = lane; it < total; it += 32) {
-                uint32_t j = 0;  // first entry whose inclusive prefix exceeds it
-#pragma unroll
-                for (uint32_t step = 16; step; step >>= 1)
-                    if (sm.pre[j + step - 1] <= it) j += step;
-                const uint64_t ent = sm.list[base + j];
-                const uint32_t excl = j ? sm.pre[j - 1] : 0u;
-                const uint32_t ql = nth_set_bit(static_cast<uint32_t>(ent), it - excl);
-                float qq[DP];
-#pragma unroll
-                for (int d = 0; d < DP; ++d) qq[d] = sm.qv[ql][d];
-                const float rq = sm.rad[ql];
-                const uint32_t bucket = static_cast<uint32_t>(ent >> 32);
-                if (heap_depth(bucket) != stop) {  // cannot happen (the walk lists buckets only); recorded
-                    stack_error = true;
-                    continue;
+                for (uint32_t o = 1; o < 32; o <<= 1) {
+                    const uint32_t v = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o) incl += v;
                 }
-                const SlotRange sr = subtree_slots(bucket, stop, p.node_depth, p.node_count, p.leaf_slots);
-                const float* slot = p.leaf + sr.first * p.leaf_stride;
-#pragma unroll 4
-                for (uint32_t s = 0; s < bucket_slots; ++s, slot += p.leaf_stride) {
-                    int32_t id;
-                    const float d2 = slot_dist<DP>(qq, slot, &id);
-                    if (id >= 0 && d2 <= rq) {
-                        // The slot is kept, not the key: half the shared memory, and the owner lane
-                        // recomputes the same distance from it when it sorts its list.
-                        const uint32_t pos = atomicAdd(&sm.cnt[ql], 1u);
-                        if (pos < C) sm.buf[pos][ql] = static_cast<uint32_t>(sr.first) + s;
+                const uint32_t total = __shfl_sync(FULL, incl, 31);
+                sm.pre[lane] = incl;
+                __syncwarp();
+                for (uint32_t it = lane; it < total; it += 32) {
+                    uint32_t j = 0;  // first entry whose inclusive prefix exceeds it
+#pragma unroll
+                    for (uint32_t step = 16; step; step >>= 1)
+                        if (sm.pre[j + step - 1] <= it) j += step;
+                    const uint64_t ent = sm.list[base + j];
+                    const uint32_t excl = j ? sm.pre[j - 1] : 0u;
+                    const uint32_t ql = nth_set_bit(static_cast<uint32_t>(ent), it - excl);
+                    float qq[DP];
+#pragma unroll
+                    for (int d = 0; d < DP; ++d) qq[d] = sm.qv[ql][d];
+                    const float rq = sm.rad[ql];
+                    const uint32_t bucket = static_cast<uint32_t>(ent >> 32);
+                    if (heap_depth(bucket) != stop) {  // cannot happen (the walk lists buckets only); recorded
+                        stack_error = true;
+                        continue;
                     }
+                    const SlotRange sr = subtree_slots(bucket, stop, p.node_depth, p.node_count, p.leaf_slots);
+                    const float* slot = p.leaf + sr.first * p.leaf_stride;
+#pragma unroll 4
+                    for (uint32_t s = 0; s < bucket_slots; ++s, slot += p.leaf_stride) {
+                        int32_t id;
+                        const float d2 = slot_dist<DP>(qq, slot, &id);
+                        if (id >= 0 && d2 <= rq) {
+                            // The slot is kept, not the key: half the shared memory, and the owner lane
+                            // recomputes the same distance from it when it sorts its list.
+                            const uint32_t pos = atomicAdd(&sm.cnt[ql], 1u);
+                            if (pos < C) sm.buf[pos][ql] = static_cast<uint32_t>(sr.first) + s;
+                        }
+                    }
+                    ++pairs;
                 }
-                ++pairs;
+                __syncwarp();
             }
-            __syncwarp();
-        }
-    };
+        };
 
-    for (uint32_t round = 0; __any_sync(FULL, pending); ++round) {
-        const float rl = pending ? r : -1.0f;
-        sm.cnt[lane] = 0;
-        sm.rad[lane] = rl;
-        __syncwarp();
-        uint32_t top = 0, nlist = 0;
-        const uint32_t m0 = __ballot_sync(FULL, box_bound<DP>(q, gp.box) <= rl);
-        if (m0) {
-            if (stop == 0) {
-                if (lane == 0) sm.list[0] = m0;
-                nlist = 1;
-            } else {
-                if (lane == 0) sm.stack[0] = 0;
-                top = 1;
-            }
-        }
-        while (top) {
+        for (uint32_t round = 0; __any_sync(FULL, pending); ++round) {
+            const float rl = pending ? r : -1.0f;
+            sm.cnt[lane] = 0;
+            sm.rad[lane] = rl;
             __syncwarp();
-            const uint32_t node = sm.stack[--top];
-            // The node's descendants `levels` below (up to 8, contiguous in the heap order) are
-            // tested at once: their box loads are independent, so they overlap in flight.
-            const uint32_t levels = min(kGroupFan, stop - heap_depth(node));
-            const uint32_t fan = 1u << levels;
-            const uint32_t first = ((node + 1) << levels) - 1;
-            uint32_t want[1u << kGroupFan];
-#pragma unroll
-            for (uint32_t j = 0; j < (1u << kGroupFan); ++j) {
-                // (j < fan first: with an unbounded radius an infinite bound is still "within".)
-                const bool in = j < fan && box_bound<DP>(q, gp.box + static_cast<size_t>(first + j) * gp.box_stride) <= rl;
-                want[j] = __ballot_sync(FULL, in);
+            uint32_t top = 0, nlist = 0;
+            const uint32_t m0 = __ballot_sync(FULL, box_bound<DP>(q, gp.box) <= rl);
+            if (m0) {
+                if (stop == 0) {
+                    if (lane == 0) sm.list[0] = m0;
+                    nlist = 1;
+                } else {
+                    if (lane == 0) sm.stack[0] = 0;
+                    top = 1;
+                }
             }
-            ++nodes;
-            if (heap_depth(node) + levels == stop) {
+            while (top) {
+                __syncwarp();
+                const uint32_t node = sm.stack[--top];
+                // The node's descendants `levels` below (up to 8, contiguous in the heap order) are
+                // tested at once: their box loads are independent, so they overlap in flight.
+                const uint32_t levels = min(kGroupFan, stop - heap_depth(node));
+                const uint32_t fan = 1u << levels;
+                const uint32_t first = ((node + 1) << levels) - 1;
+                uint32_t want[1u << kGroupFan];
 #pragma unroll
                 for (uint32_t j = 0; j < (1u << kGroupFan); ++j) {
-                    if (want[j]) {
-                        if (lane == 0) sm.list[nlist] = (static_cast<uint64_t>(first + j) << 32) | want[j];
-                        ++nlist;
-                    }
+                    // (j < fan first: with an unbounded radius an infinite bound is still "within".)
+                    const bool in = j < fan && box_bound<DP>(q, gp.box + static_cast<size_t>(first + j) * gp.box_stride) <= rl;
+                    want[j] = __ballot_sync(FULL, in);
                 }
-                if (nlist + (1u << kGroupFan) > kGroupList) {
-                    __syncwarp();
-                    scan(nlist);
-                    nlist = 0;
-                }
-            } else {
-                if (top + (1u << kGroupFan) > kGroupStack) {  // cannot happen (see kGroupStack); recorded
-                    stack_error = true;
-                    continue;
-                }
+                ++nodes;
+                if (heap_depth(node) + levels == stop) {
 #pragma unroll
-                for (uint32_t j = (1u << kGroupFan); j-- > 0;) {
-                    if (want[j]) {
-                        if (lane == 0) sm.stack[top] = first + j;
-                        ++top;
+                    for (uint32_t j = 0; j < (1u << kGroupFan); ++j) {
+                        if (want[j]) {
+                            if (lane == 0) sm.list[nlist] = (static_cast<uint64_t>(first + j) << 32) | want[j];
+                            ++nlist;
+                        }
+                    }
+                    if (nlist + (1u << kGroupFan) > kGroupList) {
+                        __syncwarp();
+                        scan(nlist);
+                        nlist = 0;
+                    }
+                } else {
+                    if (top + (1u << kGroupFan) > kGroupStack) {  // cannot happen (see kGroupStack); recorded
+                        stack_error = true;
+                        continue;
+                    }
+#pragma unroll
+                    for (uint32_t j = (1u << kGroupFan); j-- > 0;) {
+                        if (want[j]) {
+                            if (lane == 0) sm.stack[top] = first + j;
+                            ++top;
+                        }
                     }
                 }
             }
-        }
-        if (nlist) {
-            __syncwarp();
-            scan(nlist);
-        }
-        __syncwarp();
-        if (pending) {
-            const uint32_t c = sm.cnt[lane];
-            if (c > C) {
-                // More candidates than the list holds: at least k lie within r, so the per-thread
-                // search with radius r answers exactly.
-                const uint32_t pos = atomicAdd(gp.fb_count, 1u);
-                gp.fb_list[pos] = qi;
-                gp.seeds[qi] = r;
-                if (p.counters) atomicAdd(&p.counters->fallback, 1ull);
-                pending = false;
-            } else if (c >= p.k || !(r < R)) {
-                Tracker<KMAX, false, false> tr;
-                tr.init(p.k, R, nullptr, 0);
-                for (uint32_t i = 0; i < c; ++i) {
-                    int32_t id;
-                    const float d2 = slot_dist<DP>(q, p.leaf + static_cast<size_t>(sm.buf[i][lane]) * p.leaf_stride, &id);
-                    tr.offer(make_key(d2, id));
-                }
-                tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
-                pending = false;
-            } else if (round + 1 >= kGroupRounds) {
-                const uint32_t pos = atomicAdd(gp.fb_count, 1u);
-                gp.fb_list[pos] = qi;
-                gp.seeds[qi] = R;
-                if (p.counters) atomicAdd(&p.counters->fallback, 1ull);
-                pending = false;
-            } else {
-                // Fewer than k within r: grow r^2 by the volume ratio k points need at the density
-                // seen, (1.5 k / c)^(2 / dims), between 1.25 and 16.
-                const float ce = fmaxf(static_cast<float>(c), 0.5f);
-                const float g = fminf(fmaxf(exp2f(log2f(1.5f * static_cast<float>(p.k) / ce) * (2.0f / p.dims)), 1.25f),
-                                      16.0f);
-                r = fminf(R, fmaxf(r * g, 1e-30f));
+            if (nlist) {
+                __syncwarp();
+                scan(nlist);
             }
+            __syncwarp();
+            if (pending) {
+                const uint32_t c = sm.cnt[lane];
+                if (c > C) {
+                    // More candidates than the list holds: at least k lie within r, so the per-thread
+                    // search with radius r answers exactly.
+                    const uint32_t pos = atomicAdd(gp.fb_count, 1u);
+                    gp.fb_list[pos] = qi;
+                    gp.seeds[qi] = r;
+                    if (p.counters) atomicAdd(&p.counters->fallback, 1ull);
+                    pending = false;
+                } else if (c >= p.k || !(r < R)) {
+                    Tracker<KMAX, false, false> tr;
+                    tr.init(p.k, R, nullptr, 0);
+                    uint32_t i = 0;
+                    for (; i + 4 <= c; i += 4) {  // four independent slot loads in flight
+                        int32_t id[4];
+                        float d2[4];
+#pragma unroll
+                        for (uint32_t u = 0; u < 4; ++u)
+                            d2[u] = slot_dist<DP>(q, p.leaf + static_cast<size_t>(sm.buf[i + u][lane]) * p.leaf_stride, &id[u]);
+#pragma unroll
+                        for (uint32_t u = 0; u < 4; ++u) tr.offer(make_key(d2[u], id[u]));
+                    }
+                    for (; i < c; ++i) {
+                        int32_t id;
+                        const float d2 = slot_dist<DP>(q, p.leaf + static_cast<size_t>(sm.buf[i][lane]) * p.leaf_stride, &id);
+                        tr.offer(make_key(d2, id));
+                    }
+                    tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
+                    pending = false;
+                } else if (round + 1 >= kGroupRounds) {
+                    const uint32_t pos = atomicAdd(gp.fb_count, 1u);
+                    gp.fb_list[pos] = qi;
+                    gp.seeds[qi] = R;
+                    if (p.counters) atomicAdd(&p.counters->fallback, 1ull);
+                    pending = false;
+                } else {
+                    // Fewer than k within r: grow r^2 by the volume ratio k points need at the density
+                    // seen, (1.5 k / c)^(2 / dims), between 1.25 and 16.
+                    const float ce = fmaxf(static_cast<float>(c), 0.5f);
+                    const float grow = fminf(fmaxf(exp2f(log2f(1.5f * static_cast<float>(p.k) / ce) * (2.0f / p.dims)),
+                                                   1.25f), 16.0f);
+                    r = fminf(R, fmaxf(r * grow, 1e-30f));
+                }
+            }
+            __syncwarp();
         }
-        __syncwarp();
     }
     if (p.counters) {
         // nodes: walk steps (each tests up to 8 descendants); leaves: (bucket, query) pairs.
@@ -733,7 +750,8 @@ static int launch_kd_group(knn_index* ix, const QueryArgs& a, const QueryPlan& p
     gp.seed_scale = seed_scale;
     gp.fb_list = fb_list;
     gp.fb_count = fb_count;
-    KNN_TRY_CUDA(cudaMemsetAsync(fb_count, 0, sizeof(uint32_t), s));
+    gp.group_counter = fb_count + 1;  // the count's scratch slot holds 256 bytes
+    KNN_TRY_CUDA(cudaMemsetAsync(fb_count, 0, 2 * sizeof(uint32_t), s));
     if (self_seed) {
         // Subtree of at least max(4k, 32) slots.
         const uint32_t want = std::max<uint32_t>(32u, 4u * a.k);
@@ -746,7 +764,11 @@ static int launch_kd_group(knn_index* ix, const QueryArgs& a, const QueryPlan& p
     auto kern = kd_group_kernel<DP, KMAX>;
     KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     if (plan.timing) KNN_TRY(ix->timing.begin(s));
-    kern<<<ceil_div(a.count, 32 * kGroupWarps), 32 * kGroupWarps, smem, s>>>(gp);
+    int per_sm = 0;
+    KNN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kGroupWarps, smem));
+    const uint32_t grid = std::min<uint32_t>(ceil_div(a.count, 32 * kGroupWarps),
+                                             static_cast<uint32_t>(std::max(per_sm, 1) * sm_count()));
+    kern<<<grid, 32 * kGroupWarps, smem, s>>>(gp);
     KNN_LAUNCHED();
     KdParams fp = p;
     fp.order = fb_list;

@@ -358,9 +358,11 @@ size_t radix_sort_temp_bytes(uint32_t n);
 int radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt,
                      uint32_t n, int key_bits, void* temp, cudaStream_t s, bool* in_alt);
 
-// dst[i] = rows idx[i] of src ([*][dims] floats); dst_radii[i] = src_radii[idx[i]] when src_radii.
+// dst[i] = rows idx[i'] of src ([*][dims] floats); dst_radii[i] = src_radii[idx[i']] when src_radii;
+// i' = i, or with stride > 1 the i%32-th entry of the (i/32 * stride)-th run of 32 entries of idx
+// (every stride-th group of 32; the caller keeps the last index below idx's length).
 int gather_rows(const float* src, const float* src_radii, const uint32_t* idx, uint32_t count, uint32_t dims,
-                float* dst, float* dst_radii, cudaStream_t s);
+                uint32_t stride, float* dst, float* dst_radii, cudaStream_t s);
 
 // Exclusive prefix sum of per-block counts: counts[rows][cols] row-major -> out, each row
 // scanned independently (one thread block per row).

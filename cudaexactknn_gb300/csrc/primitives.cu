@@ -160,14 +160,15 @@ __global__ void fill_rows_kernel(uint32_t count, uint32_t k, float max_d2, const
     dist[i] = radii ? radii[i / k] : max_d2;
 }
 
-// dst[i] = src row idx[i] (rows of `dims` floats), and the per-row radius when given.
+// dst[i] = src row idx[i'] (rows of `dims` floats), and the per-row radius when given, where
+// i' = i, or, with stride > 1, the i%32-th entry of the (i/32 * stride)-th run of 32 entries.
 __global__ void gather_rows_kernel(const float* __restrict__ src, const float* __restrict__ src_r,
-                                   const uint32_t* __restrict__ idx, uint32_t count, uint32_t dims,
+                                   const uint32_t* __restrict__ idx, uint32_t count, uint32_t dims, uint32_t stride,
                                    float* __restrict__ dst, float* __restrict__ dst_r) {
     const uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (e >= static_cast<uint64_t>(count) * dims) return;
     const uint32_t i = static_cast<uint32_t>(e / dims), d = static_cast<uint32_t>(e % dims);
-    const uint32_t j = idx[i];
+    const uint32_t j = idx[stride > 1 ? (i / 32) * 32 * stride + i % 32 : i];
     dst[e] = src[static_cast<size_t>(j) * dims + d];
     if (src_r && d == 0) dst_r[i] = src_r[j];
 }
@@ -175,11 +176,11 @@ __global__ void gather_rows_kernel(const float* __restrict__ src, const float* _
 }  // namespace
 
 int gather_rows(const float* src, const float* src_radii, const uint32_t* idx, uint32_t count, uint32_t dims,
-                float* dst, float* dst_radii, cudaStream_t s) {
+                uint32_t stride, float* dst, float* dst_radii, cudaStream_t s) {
     if (!count) return KNN_OK;
     const uint64_t total = static_cast<uint64_t>(count) * dims;
     gather_rows_kernel<<<static_cast<uint32_t>((total + 255) / 256), 256, 0, s>>>(src, src_radii, idx, count, dims,
-                                                                                dst, dst_radii);
+                                                                                stride, dst, dst_radii);
     KNN_LAUNCHED();
     return KNN_OK;
 }
