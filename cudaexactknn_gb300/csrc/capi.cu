@@ -141,14 +141,13 @@ constexpr int kSeedRounds = 3;
 constexpr float kSeedGrowth = 16.0f;
 
 int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& plan, cudaStream_t s) {
-    // The tensor-core filter tightens each query's bound from its own cell's points; it takes the
-    // learned seed (widened) as its starting bound only when the autotuner found that faster
-    // (fewer columns pass its test before the bound is tight, against some retried queries).
-    if (plan.bf16 && !plan.tc_seeded) return dispatch(ix, a, plan, s);
+    // The tensor-core filter tightens each query's bound from its own cell's points before it
+    // skips tiles; a seed would only add retries, so it runs unseeded.
+    if (plan.bf16) return dispatch(ix, a, plan, s);
     const knn::Range range("learned-radius search");
     const size_t n = a.count;
     const uint32_t* order = nullptr;
-    if (plan.reorder && a.count >= 4096 && !plan.bf16) {
+    if (plan.reorder && a.count >= 4096) {
         if (ix->structure == KNN_KD_TREE) KNN_TRY(knn::kd_order(ix, a, s, &order));
         if (ix->structure == KNN_BALL_TREE) KNN_TRY(knn::ball_order(ix, a, s, &order));
     }
@@ -166,9 +165,6 @@ int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& p
     if (plan.group && ix->structure == KNN_KD_TREE)
         return knn::kd_group_query(ix, a, plan, order, radii, list, list_count,
                                    std::exp(0.5f * static_cast<float>(plan.widen) * ix->model_margin), s);
-    if (plan.bf16 && plan.widen)
-        KNN_TRY(knn::model_widen(radii, a.count, std::exp(0.5f * static_cast<float>(plan.widen) * ix->model_margin),
-                                 a.radii, a.max_d2, s));
     knn::QueryArgs seeded = a;
     seeded.radii = radii;
     seeded.order = order;
@@ -319,28 +315,20 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
             }
             if (rc != KNN_OK) break;
         }
-        if (try_tc) {
-            // First, so that slow tree candidates are cut short against its time; with the radius
-            // model also seeded from it (widened by exp(w m / 2), w = 1, 2).
-            for (uint32_t widen : {0u, 1u, 2u}) {
-                if (widen && !learned) break;
-                knn::QueryPlan p;
-                p.block = 128;
-                p.bf16 = true;
-                p.tc_seeded = widen > 0;
-                p.widen = widen;
-                if ((rc = consider(p)) != KNN_OK) break;
-            }
-            if (rc != KNN_OK) break;
+        if (ix->structure != KNN_BRUTE_FORCE && try_tc) {
+            // First, so that slow tree candidates are cut short against its time.
+            knn::QueryPlan p;
+            p.block = 128;
+            p.bf16 = true;
+            if ((rc = consider(p)) != KNN_OK) break;
         }
         if (ix->structure != KNN_BRUTE_FORCE) {
             for (bool warp : {false, true}) {
                 for (uint32_t leaf : {0u, 4u, 8u, 16u, 32u, 64u}) {
                     if (leaf && leaf <= ix->leaf_slots) continue;
                     knn::QueryPlan p = best;
-                    p.bf16 = p.tc_seeded = false;
+                    p.bf16 = false;
                     p.group = false;
-                    p.widen = 0;
                     p.warp = warp;
                     p.leaf_scan = leaf;
                     if ((rc = consider(p)) != KNN_OK) break;
@@ -349,10 +337,12 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
             }
             if (rc != KNN_OK) break;
         } else {
-            knn::QueryPlan p = best;
-            p.bf16 = p.tc_seeded = false;
-            p.widen = 0;
-            if ((rc = consider(p)) != KNN_OK) break;
+            if ((rc = consider(best)) != KNN_OK) break;
+            if (try_tc) {
+                knn::QueryPlan p = best;
+                p.bf16 = true;
+                if ((rc = consider(p)) != KNN_OK) break;
+            }
         }
         const knn::QueryPlan stage2 = best;
         for (uint32_t block : {32u, 64u, 256u}) {

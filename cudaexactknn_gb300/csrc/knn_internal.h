@@ -162,8 +162,7 @@ struct QueryPlan {
     bool timing = false;     // record events around the main search kernel
     bool warp = false;       // trees: warp-coherent traversal instead of one search per thread
     bool group = false;      // k-d tree: warp-group search from per-query radii (traversal 2)
-    uint32_t widen = 0;      // group search, seeded filter: learned seeds x exp(widen * margin / 2)
-    bool tc_seeded = false;  // tensor-core filter: start each query's bound from its learned seed
+    uint32_t widen = 0;      // group search: learned seeds x exp(widen * margin / 2) (fewer retries)
     bool bf16 = false;       // brute force: BF16 tensor-core filter + FP32 rescoring
     uint32_t tc_cap = 0;     // candidates kept per query by the filter (0 = default)
     uint32_t leaf_scan = 0;  // 0 = tree leaves
@@ -395,8 +394,6 @@ int model_gradients(const float* d_prm, uint32_t dims, const float* d_x, const f
 int model_predict(const float* d_prm, uint32_t dims, const float* d_x, uint32_t count, float max_d2,
                   const float* user_radii, float* d_radii, float* d_raw, cudaStream_t s,
                   bool tensor_cores = false);
-// radii[q] = min(radii[q] * scale, the caller's radius for q).
-int model_widen(float* radii, uint32_t count, float scale, const float* user_radii, float max_d2, cudaStream_t s);
 // Stable list (in `order`, or index order) of the queries that must be searched again, with
 // their seeded radii grown by `grow` (capped by the caller's radius).
 size_t retry_scratch_bytes(uint32_t count);

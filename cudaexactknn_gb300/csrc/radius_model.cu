@@ -595,21 +595,6 @@ size_t retry_scratch_bytes(uint32_t count) {
     return 2 * static_cast<size_t>(ceil_div(count, kCompactThreads)) * sizeof(uint32_t) + 512;
 }
 
-__global__ void widen_kernel(float* __restrict__ radii, uint32_t count, float scale, const float* __restrict__ user_radii,
-                             float max_d2) {
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= count) return;
-    const float cap = user_radii ? user_radii[q] : max_d2;
-    radii[q] = fminf(radii[q] * scale, cap);
-}
-
-int model_widen(float* radii, uint32_t count, float scale, const float* user_radii, float max_d2, cudaStream_t s) {
-    if (!count || scale == 1.0f) return KNN_OK;
-    widen_kernel<<<ceil_div(count, 256), 256, 0, s>>>(radii, count, scale, user_radii, max_d2);
-    KNN_LAUNCHED();
-    return KNN_OK;
-}
-
 int model_retry_list(const uint32_t* order, const int32_t* out_idx, uint32_t count, uint32_t k, float* seeded,
                      float max_d2, const float* user_radii, float grow, uint32_t* list, uint32_t* list_count,
                      void* scratch, DevCounters* counters, cudaStream_t s) {
