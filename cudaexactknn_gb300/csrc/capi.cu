@@ -116,9 +116,10 @@ int make_plan(const knn_index* ix, const knn_query_opts* o, knn::QueryPlan* p) {
     p->test_give_up = (o->flags & KNN_QF_TEST_FILTER_GIVE_UP) != 0;
     p->tc_cap = o->reserved;
     p->leaf_scan = o->leaf_scan;
-    if (o->traversal > 2) return fail(KNN_ERR_INVALID_ARGUMENT, "traversal %u: 0, 1 or 2", o->traversal);
+    if (o->traversal > 3) return fail(KNN_ERR_INVALID_ARGUMENT, "traversal %u: 0 to 3", o->traversal);
     p->warp = o->traversal == 1;
     p->group = o->traversal == 2 && ix->structure == KNN_KD_TREE;
+    p->box = o->traversal == 3 && ix->structure == KNN_KD_TREE;
     (void)ix;
     return KNN_OK;
 }
@@ -322,13 +323,25 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
             p.bf16 = true;
             if ((rc = consider(p)) != KNN_OK) break;
         }
+        if (ix->structure == KNN_KD_TREE && ix->dp <= 16) {
+            // The per-thread search over tight node boxes, by bucket size.
+            for (uint32_t leaf : {8u, 16u, 32u}) {
+                knn::QueryPlan p;
+                p.block = 128;
+                p.box = true;
+                p.leaf_scan = leaf;
+                if ((rc = consider(p)) != KNN_OK) break;
+            }
+            if (rc != KNN_OK) break;
+        }
         if (ix->structure != KNN_BRUTE_FORCE) {
             for (bool warp : {false, true}) {
                 for (uint32_t leaf : {0u, 4u, 8u, 16u, 32u, 64u}) {
                     if (leaf && leaf <= ix->leaf_slots) continue;
                     knn::QueryPlan p = best;
                     p.bf16 = false;
-                    p.group = false;
+                    p.group = p.box = false;
+                    p.widen = 0;
                     p.warp = warp;
                     p.leaf_scan = leaf;
                     if ((rc = consider(p)) != KNN_OK) break;
@@ -346,14 +359,14 @@ int autotune(knn_index* ix, const knn::QueryArgs& a, bool learned, cudaStream_t 
         }
         const knn::QueryPlan stage2 = best;
         for (uint32_t block : {32u, 64u, 256u}) {
-            if (stage2.bf16 || stage2.group) break;  // the filter and group kernels have fixed shapes
+            if (stage2.bf16 || stage2.group || stage2.box) break;  // kernels of fixed shape
             knn::QueryPlan p = stage2;
             p.block = block;
             if ((rc = consider(p)) != KNN_OK) break;
         }
         if (rc != KNN_OK) break;
         const knn::QueryPlan stage3 = best;
-        for (int v = 1; v < 8 && !stage3.bf16 && !stage3.group; ++v) {
+        for (int v = 1; v < 8 && !stage3.bf16 && !stage3.group && !stage3.box; ++v) {
             knn::QueryPlan p = stage3;
             p.heap = v & 1;
             p.sh_nn = (v >> 1) & 1;
@@ -640,7 +653,7 @@ int knn_tuned_plan(const knn_index* index, uint32_t k, uint32_t learned_radius, 
     out->shmem_tracking = slot.plan.sh_nn;
     out->shmem_stack = slot.plan.sh_stack;
     out->leaf_scan = slot.plan.leaf_scan;
-    out->traversal = slot.plan.group ? 2u : (slot.plan.warp ? 1u : 0u);
+    out->traversal = slot.plan.group ? 2u : slot.plan.box ? 3u : (slot.plan.warp ? 1u : 0u);
     out->flags = slot.plan.bf16 ? KNN_QF_BF16_FILTER : 0u;
     out->reserved = slot.candidates;
     if (ms) *ms = slot.ms;

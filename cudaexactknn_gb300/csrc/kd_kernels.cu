@@ -304,10 +304,14 @@ int kd_group_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, 
                       float* seeds, uint32_t* fb_list, uint32_t* fb_count, float seed_scale, cudaStream_t s);
 
 template <uint32_t DP>
+int kd_box_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order, cudaStream_t s);
+
+template <uint32_t DP>
 int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s) {
     const uint32_t* order = a.order;
     if (!order && p.reorder && a.count >= 4096) KNN_TRY(kd_order_dp<DP>(ix, a, s, &order));
     if (p.group && !a.count_dev) return kd_group_query_dp<DP>(ix, a, p, order, nullptr, nullptr, nullptr, 1.0f, s);
+    if (p.box) return kd_box_query_dp<DP>(ix, a, p, order, s);
     switch (k_class(a.k)) {
         case 8: return launch_kd_variant<DP, 8>(ix, a, p, order, s);
         case 16: return launch_kd_variant<DP, 16>(ix, a, p, order, s);
@@ -328,8 +332,9 @@ int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStrea
 // warp does the sum of its queries' bucket scans rather than their union.  A point within its
 // query's radius is appended to that query's candidate list in shared memory; at the end each
 // lane sorts its query's list.  A query with fewer than k candidates inside a radius below the
-// caller's grows its radius (x4 squared) and walks again; one whose list overflows, or that is
-// still short after a few rounds, goes to a list that the per-thread search answers.  Every
+// caller's grows its radius by the density it saw and walks again; one whose list overflows, or
+// that is still short after a few rounds, goes to a list that the box-bounded per-thread search
+// answers.  Every
 // answer is exact: a bucket is skipped only when its box bound exceeds the radius, and the box
 // bound is a rigorous lower bound on the float distance of every point inside (below).
 constexpr uint32_t kGroupWarps = 4;
@@ -338,7 +343,7 @@ constexpr uint32_t kGroupFan = 3;     // levels the walk descends per step (up t
 constexpr uint32_t kGroupStack = 96;  // node stack (at most 7 net entries per step, 11 steps deep)
 constexpr uint32_t kGroupRounds = 6;  // radius growth rounds before the per-thread fallback
 
-__host__ __device__ constexpr uint32_t group_cap(int kmax) { return kmax <= 8 ? 32u : (kmax <= 16 ? 64u : 96u); }
+__host__ __device__ constexpr uint32_t group_cap(int kmax) { return kmax <= 8 ? 32u : (kmax <= 16 ? 48u : 80u); }
 __host__ __device__ constexpr int box_qs(int dp) { return dp < 4 ? 4 : dp; }
 
 template <int DP, int KMAX>
@@ -557,19 +562,11 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
             __syncwarp();
             if (pending) {
                 const uint32_t c = sm.cnt[lane];
-                if (c > C) {
-                    // More candidates than the list holds: at least k lie within r, so the per-thread
-                    // search with radius r answers exactly.
-                    const uint32_t pos = atomicAdd(gp.fb_count, 1u);
-                    gp.fb_list[pos] = qi;
-                    gp.seeds[qi] = r;
-                    if (p.counters) atomicAdd(&p.counters->fallback, 1ull);
-                    pending = false;
-                } else if (c >= p.k || !(r < R)) {
-                    Tracker<KMAX, false, false> tr;
-                    tr.init(p.k, R, nullptr, 0);
+                // The k smallest keys among the first n listed candidates (their distances
+                // recomputed from the slots, four loads in flight).
+                auto select = [&](Tracker<KMAX, false, false>& tr, uint32_t n) {
                     uint32_t i = 0;
-                    for (; i + 4 <= c; i += 4) {  // four independent slot loads in flight
+                    for (; i + 4 <= n; i += 4) {
                         int32_t id[4];
                         float d2[4];
 #pragma unroll
@@ -578,11 +575,29 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
 #pragma unroll
                         for (uint32_t u = 0; u < 4; ++u) tr.offer(make_key(d2[u], id[u]));
                     }
-                    for (; i < c; ++i) {
+                    for (; i < n; ++i) {
                         int32_t id;
                         const float d2 = slot_dist<DP>(q, p.leaf + static_cast<size_t>(sm.buf[i][lane]) * p.leaf_stride, &id);
                         tr.offer(make_key(d2, id));
                     }
+                };
+                if (c > C) {
+                    // More candidates than the list holds.  The k-th smallest distance among the C
+                    // kept bounds the k-th neighbour's (k real points lie within it): the
+                    // per-thread search starts from it.  (Walking again with a radius shrunk by the
+                    // density was tried: the extra rounds cost more than the searches they save.)
+                    Tracker<KMAX, false, false> tr;
+                    tr.init(p.k, r, nullptr, 0);
+                    select(tr, C);
+                    const uint32_t pos = atomicAdd(gp.fb_count, 1u);
+                    gp.fb_list[pos] = qi;
+                    gp.seeds[qi] = fminf(tr.radius(), r);
+                    if (p.counters) atomicAdd(&p.counters->fallback, 1ull);
+                    pending = false;
+                } else if (c >= p.k || !(r < R)) {
+                    Tracker<KMAX, false, false> tr;
+                    tr.init(p.k, R, nullptr, 0);
+                    select(tr, c);
                     tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
                     pending = false;
                 } else if (round + 1 >= kGroupRounds) {
@@ -616,12 +631,79 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGrou
     }
 }
 
-// Per-thread search of the queries the group search left over (grid-stride over the list).
+// Per-thread search over the tight node boxes (traversal 3, and the group search's leftovers):
+// depth first, the closer child first, a node skipped when its box bound exceeds the current k-th
+// distance, buckets at depth `stop` scanned whole; from radius r2, results to the query's row.
+// Box bounds matter most far from the data, where a single splitting plane prunes little.
 template <int DP, int KMAX>
-__global__ void __launch_bounds__(128) kd_fallback_kernel(const KdParams p) {
-    const uint32_t n = *p.count_dev;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
-        kd_search_thread<DP, KMAX, false, false, false>(p, t, nullptr);
+__device__ __forceinline__ void kd_box_search(const KdParams& p, const float* __restrict__ box, uint32_t box_stride,
+                                              uint32_t stop, uint32_t qi, float r2) {
+    float q[DP];
+    load_query<DP>(p.queries, p.dims, qi, q);
+    Tracker<KMAX, false, false> tr;
+    tr.init(p.k, r2, nullptr, 0);
+    Stack<false> st;
+    st.init(nullptr, 0);
+    st.push(0, box_bound<DP>(q, box));
+    bool overflow = false;
+    LocalCounters lc;
+    while (st.top) {
+        uint32_t node;
+        float bound;
+        st.pop(&node, &bound);
+        if (bound > tr.radius()) continue;
+        if (heap_depth(node) == stop) {
+            const SlotRange sr = subtree_slots(node, stop, p.node_depth, p.node_count, p.leaf_slots);
+            const float* slot = p.leaf + sr.first * p.leaf_stride;
+            ++lc.leaves;
+            for (uint32_t s = 0; s < sr.count; ++s, slot += p.leaf_stride) {
+                int32_t id;
+                const float d2 = slot_dist<DP>(q, slot, &id);
+                if (id < 0) continue;
+                ++lc.points;
+                tr.offer(make_key(d2, id));
+            }
+            continue;
+        }
+        ++lc.nodes;
+        const uint32_t l = 2 * node + 1;
+        const float bl = box_bound<DP>(q, box + static_cast<size_t>(l) * box_stride);
+        const float br = box_bound<DP>(q, box + static_cast<size_t>(l + 1) * box_stride);
+        const bool left_first = bl <= br;  // pushed last, popped first
+        const uint32_t far_node = left_first ? l + 1 : l, near_node = left_first ? l : l + 1;
+        const float far_b = left_first ? br : bl, near_b = left_first ? bl : br;
+        if (far_b <= tr.radius()) overflow |= !st.push(far_node, far_b);
+        if (near_b <= tr.radius()) overflow |= !st.push(near_node, near_b);
+    }
+    tr.emit(p.k, p.out_idx + static_cast<size_t>(qi) * p.k, p.out_dist + static_cast<size_t>(qi) * p.k);
+    if (p.counters) {
+        lc.flush(p.counters);
+        if (overflow) atomicExch(&p.counters->error, 1);
+    }
+}
+
+// The group search's leftovers, from each one's radius in `seeds`: one query per warp (lane 0),
+// warps striding over the list.  The leftovers lie scattered in space, so 32 of them in one warp
+// would take 32 different paths one after another; a warp each runs them side by side.
+template <int DP, int KMAX>
+__global__ void __launch_bounds__(128) kd_fallback_kernel(const KdGroupParams gp) {
+    if ((threadIdx.x & 31u) != 0) return;
+    const uint32_t n = *gp.fb_count;
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t t = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; t < n; t += warps) {
+        const uint32_t qi = gp.fb_list[t];
+        kd_box_search<DP, KMAX>(gp.p, gp.box, gp.box_stride, gp.p.stop_depth, qi, gp.seeds[qi]);
+    }
+}
+
+// Traversal 3: one box-bounded search per thread, in the batch's locality order.
+template <int DP, int KMAX>
+__global__ void __launch_bounds__(128) kd_box_knn_kernel(const KdParams p, const float* __restrict__ box,
+                                                         uint32_t box_stride) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (p.count_dev ? *p.count_dev : p.nq)) return;
+    const uint32_t qi = p.order ? p.order[t] - p.order_base : t;
+    kd_box_search<DP, KMAX>(p, box, box_stride, p.stop_depth, qi, p.radii ? p.radii[qi] : p.max_d2);
 }
 
 // Self seeds: each query's k-th distance among the points of the subtree of at least
@@ -770,14 +852,61 @@ static int launch_kd_group(knn_index* ix, const QueryArgs& a, const QueryPlan& p
                                              static_cast<uint32_t>(std::max(per_sm, 1) * sm_count()));
     kern<<<grid, 32 * kGroupWarps, smem, s>>>(gp);
     KNN_LAUNCHED();
-    KdParams fp = p;
-    fp.order = fb_list;
-    fp.count_dev = fb_count;
-    fp.radii = seeds;
-    kd_fallback_kernel<DP, KMAX><<<2 * static_cast<uint32_t>(sm_count()), 128, 0, s>>>(fp);
+    kd_fallback_kernel<DP, KMAX><<<8 * static_cast<uint32_t>(sm_count()), 128, 0, s>>>(gp);
     KNN_LAUNCHED();
     if (plan.timing) KNN_TRY(ix->timing.end(s));
     return KNN_OK;
+}
+
+// Builds the node boxes on first use (down to subtrees of at most 4 slots).
+template <uint32_t DP>
+int kd_box_ensure(knn_index* ix, cudaStream_t s) {
+    if (ix->kd_box.ptr) return KNN_OK;
+    ix->kd_box_depth = scan_depth_for(ix->node_depth, ix->leaf_slots, 4);
+    return kd_box_build_dp<DP>(ix, s);
+}
+
+// Traversal 3 (plan.box): per-thread box-bounded search, buckets of plan.leaf_scan slots (0 = 8).
+template <uint32_t DP>
+int kd_box_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order, cudaStream_t s) {
+    if constexpr (DP > 16) {
+        return fail(KNN_ERR_INVALID_ARGUMENT, "box search: dims above 16");
+    } else {
+        KNN_TRY(kd_box_ensure<DP>(ix, s));
+        KdParams p{};
+        p.split = ix->split.as<float>();
+        p.leaf = ix->leaf.as<float>();
+        p.leaf_stride = ix->leaf_stride;
+        p.node_count = ix->node_count;
+        p.node_depth = ix->node_depth;
+        p.stop_depth = std::min(scan_depth_for(ix->node_depth, ix->leaf_slots, plan.leaf_scan ? plan.leaf_scan : 8u),
+                                ix->kd_box_depth);
+        p.leaf_slots = ix->leaf_slots;
+        p.aux = ix->aux_dims;
+        p.queries = a.queries;
+        p.dims = ix->dims;
+        p.nq = a.count;
+        p.order = order;
+        p.count_dev = a.count_dev;
+        p.max_d2 = a.max_d2;
+        p.radii = a.radii;
+        p.k = a.k;
+        p.out_idx = a.out_idx;
+        p.out_dist = a.out_dist;
+        p.counters = a.counters;
+        const uint32_t grid = ceil_div(a.count, 128);
+        if (plan.timing) KNN_TRY(ix->timing.begin(s));
+        switch (k_class(a.k)) {
+            case 8: kd_box_knn_kernel<DP, 8><<<grid, 128, 0, s>>>(p, ix->kd_box.as<float>(), ix->kd_box_stride); break;
+            case 16: kd_box_knn_kernel<DP, 16><<<grid, 128, 0, s>>>(p, ix->kd_box.as<float>(), ix->kd_box_stride); break;
+            case 32: kd_box_knn_kernel<DP, 32><<<grid, 128, 0, s>>>(p, ix->kd_box.as<float>(), ix->kd_box_stride); break;
+            case 64: kd_box_knn_kernel<DP, 64><<<grid, 128, 0, s>>>(p, ix->kd_box.as<float>(), ix->kd_box_stride); break;
+            default: kd_box_knn_kernel<DP, 128><<<grid, 128, 0, s>>>(p, ix->kd_box.as<float>(), ix->kd_box_stride); break;
+        }
+        KNN_LAUNCHED();
+        if (plan.timing) KNN_TRY(ix->timing.end(s));
+        return KNN_OK;
+    }
 }
 
 // Warp-group search (plan.group) with per-query seeds (or self seeds when `seeds` holds none):
@@ -790,10 +919,7 @@ int kd_group_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, 
         return fail(KNN_ERR_INVALID_ARGUMENT, "group search: dims above 16");
     } else {
         if (a.k > 32) return fail(KNN_ERR_INVALID_ARGUMENT, "group search: k above 32");
-        if (!ix->kd_box.ptr) {
-            ix->kd_box_depth = scan_depth_for(ix->node_depth, ix->leaf_slots, 4);
-            KNN_TRY(kd_box_build_dp<DP>(ix, s));
-        }
+        KNN_TRY(kd_box_ensure<DP>(ix, s));
         const bool self_seed = seeds == nullptr;
         const size_t n = a.count;
         if (self_seed) {
@@ -812,6 +938,7 @@ int kd_group_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, 
 }
 
 template int kd_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
+template int kd_box_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, cudaStream_t);
 template int kd_group_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, float*,
                                         uint32_t*, uint32_t*, float, cudaStream_t);
 template int kd_order_dp<KNN_DP>(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);

@@ -162,6 +162,7 @@ struct QueryPlan {
     bool timing = false;     // record events around the main search kernel
     bool warp = false;       // trees: warp-coherent traversal instead of one search per thread
     bool group = false;      // k-d tree: warp-group search from per-query radii (traversal 2)
+    bool box = false;        // k-d tree: per-thread search over tight node boxes (traversal 3)
     uint32_t widen = 0;      // group search: learned seeds x exp(widen * margin / 2) (fewer retries)
     bool bf16 = false;       // brute force: BF16 tensor-core filter + FP32 rescoring
     uint32_t tc_cap = 0;     // candidates kept per query by the filter (0 = default)

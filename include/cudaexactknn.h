@@ -111,7 +111,8 @@ typedef struct knn_query_opts {
                                warp's 32 queries walk the tree once against tight node boxes from
                                per-query radii -- the radius model's seeds, or each query's own
                                subtree -- and share out their (bucket, query) scans; leaf_scan =
-                               points per bucket, 0 = 8) */
+                               points per bucket, 0 = 8); 3 = one search per thread bounded by
+                               the same tight node boxes instead of splitting planes */
     uint32_t reserved;      /* KNN_QF_BF16_FILTER: candidates kept per query (0 = the engine's
                                default, min(4096, max(1024, 16 k))); for
                                knn_tuned_plan, the number of candidate plans timed */

@@ -1,5 +1,6 @@
 """The k-d tree's warp-group search (traversal 2): a warp's 32 queries walk the tree once against
-tight node boxes from per-query radii and share out their bucket scans.  Every row must equal the
+tight node boxes from per-query radii and share out their bucket scans; and the per-thread search
+over the same boxes (traversal 3).  Every row must equal the
 oracle's brute force exactly (sorted u64 keys), whether the radii come from each query's own
 subtree or from the radius model, with a caller's radius, per-query radii, ties, duplicates that
 overflow a query's candidate list, and point sets smaller than k."""
@@ -33,6 +34,10 @@ def test_group_self_seeded_dims(dims, skips):
             got = gu.run(ix, qs, k, traversal=2, leaf_scan=leaf)
             gu.assert_sorted_rows(*got)
             gu.assert_rows_equal(*got, *want, what=f"D={dims} skips={skips} k={k} leaf={leaf}")
+            gu.assert_rows_equal(*gu.run(ix, qs, k, traversal=3, leaf_scan=leaf), *want,
+                                 what=f"box D={dims} skips={skips} k={k} leaf={leaf}")
+    for k in (33, 64, 128):  # the box search takes every k
+        gu.assert_rows_equal(*gu.run(ix, qs[:500], k, traversal=3), *_want(pts, qs[:500], k), what=f"box D={dims} k={k}")
     ix.close()
 
 
@@ -45,6 +50,7 @@ def test_group_mixture_and_radius(k):
     gu.assert_rows_equal(*gu.run(ix, qs, k, traversal=2), *_want(pts, qs, k), what=f"mixture k={k}")
     r2 = 2e-5
     gu.assert_rows_equal(*gu.run(ix, qs, k, r2, traversal=2), *_want(pts, qs, k, r2), what=f"radius k={k}")
+    gu.assert_rows_equal(*gu.run(ix, qs, k, traversal=3), *_want(pts, qs, k), what=f"box k={k}")
     ix.close()
 
 
@@ -84,8 +90,9 @@ def test_group_ties_and_overflowing_duplicates():
     qs = np.concatenate([g[rng.choice(len(g), 2000)], dup[::50], (g[:500] + 0.5 / 24)]).astype(np.float32)
     ix = gu.make_index("kd", pts, 0)
     for k in (1, 6, 16, 32):
-        got = gu.run(ix, qs, k, traversal=2)
-        gu.assert_rows_equal(*got, *_want(pts, qs, k), what=f"ties k={k}")
+        want = _want(pts, qs, k)
+        gu.assert_rows_equal(*gu.run(ix, qs, k, traversal=2), *want, what=f"ties k={k}")
+        gu.assert_rows_equal(*gu.run(ix, qs, k, traversal=3), *want, what=f"box ties k={k}")
     st = ix.stats(knn.Query(gu.to_dev(qs), len(qs), INF), 16, traversal=2)
     assert st.fallback_queries >= len(dup[::50]), st.fallback_queries
     ix.close()
@@ -101,6 +108,8 @@ def test_group_small_sets(n):
         gu.assert_rows_equal(*gu.run(ix, qs, k, traversal=2), *_want(pts, qs, k), what=f"n={n} k={k}")
         gu.assert_rows_equal(*gu.run(ix, qs, k, 0.01, traversal=2), *_want(pts, qs, k, 0.01),
                              what=f"n={n} k={k} r2=0.01")
+        gu.assert_rows_equal(*gu.run(ix, qs, k, 0.01, traversal=3), *_want(pts, qs, k, 0.01),
+                             what=f"box n={n} k={k} r2=0.01")
     ix.close()
 
 
