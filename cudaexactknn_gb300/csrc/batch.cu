@@ -27,7 +27,7 @@
 namespace knn {
 
 template <uint32_t DP>
-int kd_batch_launch(const void*, uint32_t, uint32_t, uint32_t, uint32_t, bool, uint32_t, uint32_t*, uint32_t*,
+int kd_batch_launch(const void*, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t*, uint32_t*,
                     uint32_t*, bool, cudaStream_t);
 template <uint32_t DP>
 int ball_batch_launch(const void*, uint32_t, uint32_t, uint32_t, uint32_t, bool, uint32_t, uint32_t*, uint32_t*,
@@ -43,15 +43,16 @@ int query_structure(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaS
 
 namespace {
 
+// mode: 0 per-thread search, 1 warp-coherent, 2 box search (k-d only).
 int batch_launch(int structure, uint32_t dp, const void* sets, uint32_t nsets, uint32_t total_queries,
-                 uint32_t total_blocks, uint32_t kmax, bool warp, uint32_t block, uint32_t* counter, uint32_t* keys,
+                 uint32_t total_blocks, uint32_t kmax, uint32_t mode, uint32_t block, uint32_t* counter, uint32_t* keys,
                  uint32_t* vals, bool key_pass, cudaStream_t s) {
 #define KNN_BL(D_)                                                                                                  \
     case D_:                                                                                                        \
         return structure == KNN_KD_TREE                                                                             \
-                   ? kd_batch_launch<D_>(sets, nsets, total_queries, total_blocks, kmax, warp, block, counter, keys, \
+                   ? kd_batch_launch<D_>(sets, nsets, total_queries, total_blocks, kmax, mode, block, counter, keys, \
                                          vals, key_pass, s)                                                         \
-                   : ball_batch_launch<D_>(sets, nsets, total_queries, total_blocks, kmax, warp, block, counter,    \
+                   : ball_batch_launch<D_>(sets, nsets, total_queries, total_blocks, kmax, mode == 1, block, counter, \
                                            keys, vals, key_pass, s);
     switch (dp) {
         KNN_BL(1) KNN_BL(2) KNN_BL(3) KNN_BL(4) KNN_BL(8) KNN_BL(16) KNN_BL(32) KNN_BL(64) KNN_BL(128)
@@ -96,11 +97,13 @@ namespace {
 
 using knn::fail;
 
+uint32_t class_mode(const knn_batch::Class& c) { return c.plan.box ? 2u : c.plan.warp ? 1u : 0u; }
+
 // Enqueues one class: locality sort (key pass + radix sort) then the persistent search kernel.
 int enqueue_class(knn_batch::Class& c, cudaStream_t s) {
     if (c.sort) {
         KNN_TRY(knn::batch_launch(c.structure, c.dp, c.sets.ptr, static_cast<uint32_t>(c.items.size()), c.total_queries,
-                                  c.total_blocks, c.kmax, c.plan.warp, c.plan.block, c.counter, c.keys, c.vals, true, s));
+                                  c.total_blocks, c.kmax, class_mode(c), c.plan.block, c.counter, c.keys, c.vals, true, s));
         bool in_alt = false;
         KNN_TRY(knn::radix_sort_pairs(c.keys, c.vals, c.keys_alt, c.vals_alt, c.total_queries,
                                       static_cast<int>(c.key_bits), c.sort_temp, s, &in_alt));
@@ -108,7 +111,7 @@ int enqueue_class(knn_batch::Class& c, cudaStream_t s) {
     }
     KNN_TRY_CUDA(cudaMemsetAsync(c.counter, 0, sizeof(uint32_t), s));
     return knn::batch_launch(c.structure, c.dp, c.sets.ptr, static_cast<uint32_t>(c.items.size()), c.total_queries,
-                             c.total_blocks, c.kmax, c.plan.warp, c.plan.block, c.counter, c.keys, c.vals, false, s);
+                             c.total_blocks, c.kmax, class_mode(c), c.plan.block, c.counter, c.keys, c.vals, false, s);
 }
 
 knn::QueryArgs item_args(const knn_batch_item& it) {
@@ -235,6 +238,12 @@ int batch_create(const knn_batch_item* items, uint32_t count, uint32_t flags, vo
                 break;
             }
             continue;
+        }
+        if (c.plan.box) {
+            // The box search reads each index's node boxes: build them now (capture cannot allocate).
+            for (uint32_t i : c.items)
+                if ((rc = knn::kd_box_prepare(items[i].index, s)) != KNN_OK) break;
+            if (rc != KNN_OK) break;
         }
         const uint32_t block = c.plan.block;
         uint32_t first_block = 0;

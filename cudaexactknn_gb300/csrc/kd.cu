@@ -22,6 +22,8 @@ int kd_order_dp(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
 template <uint32_t DP>
 int kd_group_query_dp(knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, float*, uint32_t*, uint32_t*,
                       float, cudaStream_t);
+template <uint32_t DP>
+int kd_box_prepare_dp(knn_index*, cudaStream_t);
 
 namespace {
 
@@ -155,6 +157,18 @@ int kd_group_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, const 
         case 8: return kd_group_query_dp<8>(ix, a, p, order, seeds, fb_list, fb_count, seed_scale, s);
         case 16: return kd_group_query_dp<16>(ix, a, p, order, seeds, fb_list, fb_count, seed_scale, s);
         default: return fail(KNN_ERR_INVALID_ARGUMENT, "group search: dims above 16");
+    }
+}
+
+int kd_box_prepare(knn_index* ix, cudaStream_t s) {
+    switch (ix->dp) {
+        case 1: return kd_box_prepare_dp<1>(ix, s);
+        case 2: return kd_box_prepare_dp<2>(ix, s);
+        case 3: return kd_box_prepare_dp<3>(ix, s);
+        case 4: return kd_box_prepare_dp<4>(ix, s);
+        case 8: return kd_box_prepare_dp<8>(ix, s);
+        case 16: return kd_box_prepare_dp<16>(ix, s);
+        default: return fail(KNN_ERR_INVALID_ARGUMENT, "box search: dims above 16");
     }
 }
 

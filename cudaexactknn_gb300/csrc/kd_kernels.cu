@@ -858,6 +858,9 @@ static int launch_kd_group(knn_index* ix, const QueryArgs& a, const QueryPlan& p
     return KNN_OK;
 }
 
+template <uint32_t DP>
+int kd_box_prepare_dp(knn_index* ix, cudaStream_t s);
+
 // Builds the node boxes on first use (down to subtrees of at most 4 slots).
 template <uint32_t DP>
 int kd_box_ensure(knn_index* ix, cudaStream_t s) {
@@ -939,6 +942,11 @@ int kd_group_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, 
 
 template int kd_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
 template int kd_box_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, cudaStream_t);
+template <>
+int kd_box_prepare_dp<KNN_DP>(knn_index* ix, cudaStream_t s) {
+    if constexpr (KNN_DP > 16) return fail(KNN_ERR_INVALID_ARGUMENT, "box search: dims above 16");
+    else return kd_box_ensure<KNN_DP>(ix, s);
+}
 template int kd_group_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, float*,
                                         uint32_t*, uint32_t*, float, cudaStream_t);
 template int kd_order_dp<KNN_DP>(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
@@ -950,6 +958,8 @@ struct KdBatchSet {
     uint32_t first_block;  // first work block of this set in the class
     uint32_t query_offset; // first query of this set in the class-wide numbering
     uint32_t levels;       // descent depth of the locality key
+    const float* box;      // the index's node boxes (box-search classes), or null
+    uint32_t box_stride;
 };
 
 __device__ __forceinline__ uint32_t kd_find_set(const KdBatchSet* sets, uint32_t nsets, uint32_t item, bool by_query) {
@@ -984,7 +994,8 @@ __global__ void kd_batch_key_kernel(const KdBatchSet* __restrict__ sets, uint32_
 
 // Persistent kernel: blocks take work blocks (blockDim queries of one set) from a shared counter
 // until the class is done; sets of very different sizes share the GPU without a launch each.
-template <int DP, int KMAX, bool WARP>
+// MODE: 0 per-thread search, 1 warp-coherent search, 2 per-thread box search (dims <= 16).
+template <int DP, int KMAX, int MODE>
 __global__ void __launch_bounds__(256) kd_batch_kernel(const KdBatchSet* __restrict__ sets, uint32_t nsets,
                                                         uint32_t total_blocks, uint32_t* __restrict__ counter) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -998,8 +1009,14 @@ __global__ void __launch_bounds__(256) kd_batch_kernel(const KdBatchSet* __restr
         const uint32_t si = kd_find_set(sets, nsets, item, false);
         const KdParams& p = sets[si].p;
         const uint32_t t = (item - sets[si].first_block) * blockDim.x + threadIdx.x;
-        if constexpr (WARP) {
+        if constexpr (MODE == 1) {
             kd_search_warp<DP, KMAX, false, false, false>(p, t, p.nq, smem);
+        } else if constexpr (MODE == 2 && DP <= 16) {
+            if (t < p.nq) {
+                const uint32_t qi = p.order ? p.order[t] - p.order_base : t;
+                kd_box_search<DP, KMAX>(p, sets[si].box, sets[si].box_stride, p.stop_depth, qi,
+                                        p.radii ? p.radii[qi] : p.max_d2);
+            }
         } else {
             if (t < p.nq) kd_search_thread<DP, KMAX, false, false, false>(p, t, smem);
         }
@@ -1008,7 +1025,7 @@ __global__ void __launch_bounds__(256) kd_batch_kernel(const KdBatchSet* __restr
 
 template <uint32_t DP>
 int kd_batch_launch(const void* sets, uint32_t nsets, uint32_t total_queries, uint32_t total_blocks, uint32_t kmax,
-                       bool warp, uint32_t block, uint32_t* counter, uint32_t* keys, uint32_t* vals, bool key_pass,
+                       uint32_t mode, uint32_t block, uint32_t* counter, uint32_t* keys, uint32_t* vals, bool key_pass,
                        cudaStream_t s) {
     using Set = KdBatchSet;
     const Set* d_sets = static_cast<const Set*>(sets);
@@ -1018,7 +1035,7 @@ int kd_batch_launch(const void* sets, uint32_t nsets, uint32_t total_queries, ui
         return KNN_OK;
     }
 #define KNN_BATCH(KM, W)                                                                              \
-    if (kmax == KM && warp == W) {                                                                    \
+    if (kmax == KM && mode == W) {                                                                    \
         auto kern = kd_batch_kernel<DP, KM, W>;                                                    \
         int per_sm = 0;                                                                               \
         KNN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0));         \
@@ -1027,8 +1044,9 @@ int kd_batch_launch(const void* sets, uint32_t nsets, uint32_t total_queries, ui
         KNN_LAUNCHED();                                                                               \
         return KNN_OK;                                                                                \
     }
-    KNN_BATCH(8, false) KNN_BATCH(16, false) KNN_BATCH(32, false) KNN_BATCH(64, false) KNN_BATCH(128, false)
-    KNN_BATCH(8, true) KNN_BATCH(16, true) KNN_BATCH(32, true) KNN_BATCH(64, true) KNN_BATCH(128, true)
+    KNN_BATCH(8, 0) KNN_BATCH(16, 0) KNN_BATCH(32, 0) KNN_BATCH(64, 0) KNN_BATCH(128, 0)
+    KNN_BATCH(8, 1) KNN_BATCH(16, 1) KNN_BATCH(32, 1) KNN_BATCH(64, 1) KNN_BATCH(128, 1)
+    KNN_BATCH(8, 2) KNN_BATCH(16, 2) KNN_BATCH(32, 2) KNN_BATCH(64, 2) KNN_BATCH(128, 2)
 #undef KNN_BATCH
     return fail(KNN_ERR_INVALID_ARGUMENT, "batch class k %u", kmax);
 }
@@ -1061,11 +1079,17 @@ void kd_batch_set_fill(void* out, const knn_index* ix, const QueryArgs& a, const
     bs.first_block = first_block;
     bs.query_offset = query_offset;
     bs.levels = std::min<uint32_t>(ix->node_depth, 24);
+    if (plan.box && ix->kd_box.ptr) {  // prepared by kd_box_prepare before the batch is captured
+        bs.box = ix->kd_box.as<float>();
+        bs.box_stride = ix->kd_box_stride;
+        p.stop_depth = std::min(scan_depth_for(ix->node_depth, ix->leaf_slots, plan.leaf_scan ? plan.leaf_scan : 8u),
+                                ix->kd_box_depth);
+    }
     std::memcpy(out, &bs, sizeof(bs));
 }
 #endif
 
-template int kd_batch_launch<KNN_DP>(const void*, uint32_t, uint32_t, uint32_t, uint32_t, bool, uint32_t, uint32_t*,
+template int kd_batch_launch<KNN_DP>(const void*, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t*,
                                       uint32_t*, uint32_t*, bool, cudaStream_t);
 
 }  // namespace knn

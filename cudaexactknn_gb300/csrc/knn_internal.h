@@ -418,6 +418,8 @@ int ball_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t
 int kd_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 // Warp-group k-d search from per-query seed radii (kd_kernels.cu); queries it cannot settle go to
 // fb_list / fb_count and are answered by the per-thread search in the same call.
+// The k-d node boxes the box and group searches read, built if missing (dims <= 16).
+int kd_box_prepare(knn_index* ix, cudaStream_t s);
 int kd_group_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, const uint32_t* order, float* seeds,
                    uint32_t* fb_list, uint32_t* fb_count, float seed_scale, cudaStream_t s);
 int ball_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
