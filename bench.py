@@ -469,7 +469,7 @@ def measure(D, w, key, steps, warmup, plain_steps, world, rank, cpu=True):
         return dict(bf16_filter=bool(tuned.flags & _lib.QF_BF16_FILTER), block_size=tuned.block_size,
                     heap=bool(tuned.heap_tracking), shmem_tracking=bool(tuned.shmem_tracking),
                     shmem_stack=bool(tuned.shmem_stack), leaf_scan=tuned.leaf_scan,
-                    traversal={0: "thread", 1: "warp", 2: "group"}.get(tuned.traversal, str(tuned.traversal)),
+                    traversal={0: "thread", 1: "warp", 2: "group", 3: "box"}.get(tuned.traversal, str(tuned.traversal)),
                     candidates_timed=tuned.reserved)
 
     tuned_plan = plan_of(learned)
@@ -516,6 +516,8 @@ def measure(D, w, key, steps, warmup, plain_steps, world, rank, cpu=True):
     kernel_name = {"kd": "kd_knn_kernel", "ball": "ball_knn_kernel", "bf": "bf_knn_kernel"}[w.structure]
     if tuned_plan["traversal"] == "group":
         kernel_name = "kd_group_kernel"
+    elif tuned_plan["traversal"] == "box":
+        kernel_name = "kd_box_knn_kernel"
     if tuned_plan["bf16_filter"]:
         # Tensor-core filter: the MMA work it issues, 2 x 128 queries x 256 rows x (16 per K step,
         # ceil(D/16) steps) per point tile scanned (device counter), against the dense 16-bit peak.
