@@ -696,6 +696,141 @@ __global__ void __launch_bounds__(128) kd_fallback_kernel(const KdGroupParams gp
     }
 }
 
+// ---- one query per warp: the group search's leftovers -----------------------------------------
+// The leftovers are mostly queries far from the data (their k-th distance is large and the ball
+// brushes many buckets of a dense cluster) or queries whose seed held far more points than a
+// list: searched by one thread each they took up to ~0.6 ms apiece and set the length of the
+// whole pass.  Here a warp searches one of them: each step tests the up-to-32 descendants five
+// levels below a node, one per lane (the box bound against the current k-th distance), scans the
+// wanted buckets one per lane, and merges the candidates into a top-32 held across the warp
+// (lane i the i-th smallest key) by bitonic sorting networks over shuffles.  Exact as the other
+// searches: a subtree is skipped only when its box bound exceeds the current k-th distance.
+constexpr uint32_t kSoloFan = 5;     // levels per step: up to 32 descendants, one per lane
+constexpr uint32_t kSoloStack = 256; // at most 31 net entries per step, 7 steps deep
+constexpr uint32_t kSoloCand = 1024; // candidates of one step: 32 buckets of at most 32 slots
+
+struct SoloWarpSmem {
+    uint64_t cand[kSoloCand];
+    uint32_t stack[kSoloStack];
+    uint32_t ncand;
+};
+
+__device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, uint32_t m) {
+    const uint32_t lo = __shfl_xor_sync(0xFFFFFFFFu, static_cast<uint32_t>(v), m);
+    const uint32_t hi = __shfl_xor_sync(0xFFFFFFFFu, static_cast<uint32_t>(v >> 32), m);
+    return (static_cast<uint64_t>(hi) << 32) | lo;
+}
+
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, uint32_t src) {
+    const uint32_t lo = __shfl_sync(0xFFFFFFFFu, static_cast<uint32_t>(v), src);
+    const uint32_t hi = __shfl_sync(0xFFFFFFFFu, static_cast<uint32_t>(v >> 32), src);
+    return (static_cast<uint64_t>(hi) << 32) | lo;
+}
+
+// Ascending bitonic sort of 32 keys, one per lane.
+__device__ __forceinline__ uint64_t warp_sort64(uint64_t v, uint32_t lane) {
+#pragma unroll
+    for (uint32_t k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            const uint64_t o = shfl_xor64(v, j);
+            const bool up = (lane & k) == 0, lower = (lane & j) == 0;
+            v = (lower == up) ? (v < o ? v : o) : (v < o ? o : v);
+        }
+    }
+    return v;
+}
+
+// The 32 smallest of two ascending 32-key sequences (one key per lane each), ascending.
+__device__ __forceinline__ uint64_t warp_merge_low64(uint64_t a, uint64_t b, uint32_t lane) {
+    const uint64_t rb = shfl64(b, 31 - lane);
+    uint64_t v = a < rb ? a : rb;  // a bitonic sequence holding the 32 smallest
+#pragma unroll
+    for (uint32_t j = 16; j > 0; j >>= 1) {
+        const uint64_t o = shfl_xor64(v, j);
+        v = (lane & j) == 0 ? (v < o ? v : o) : (v < o ? o : v);
+    }
+    return v;
+}
+
+template <int DP, int KMAX>
+__global__ void __launch_bounds__(128) kd_solo_kernel(const KdGroupParams gp) {
+    static_assert(KMAX <= 32, "the top-k is held one key per lane");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SoloWarpSmem& sm = reinterpret_cast<SoloWarpSmem*>(smem_raw)[threadIdx.x >> 5];
+    const KdParams& p = gp.p;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t stop = p.stop_depth;
+    const uint32_t n = *gp.fb_count;
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    LocalCounters lc;
+    bool stack_error = false;
+    for (uint32_t t = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; t < n; t += warps) {
+        const uint32_t qi = gp.fb_list[t];
+        float q[DP];
+        load_query<DP>(p.queries, p.dims, qi, q);
+        const float r2 = gp.seeds[qi];
+        uint64_t top = make_key(r2, -1);  // lane i: the i-th smallest key so far
+        float kth = r2;
+        if (lane == 0) sm.stack[0] = 0;
+        uint32_t depth_n = 1;  // stack entries
+        while (depth_n) {
+            __syncwarp();
+            const uint32_t node = sm.stack[--depth_n];
+            const uint32_t levels = min(kSoloFan, stop - heap_depth(node));
+            const uint32_t fan = 1u << levels;
+            const uint32_t first = ((node + 1) << levels) - 1;
+            const bool want =
+                lane < fan && box_bound<DP>(q, gp.box + static_cast<size_t>(first + lane) * gp.box_stride) <= kth;
+            const uint32_t wm = __ballot_sync(0xFFFFFFFFu, want);
+            if (heap_depth(node) + levels == stop) {
+                if (lane == 0) sm.ncand = 0;
+                __syncwarp();
+                if (want) {
+                    const SlotRange sr = subtree_slots(first + lane, stop, p.node_depth, p.node_count, p.leaf_slots);
+                    const float* slot = p.leaf + sr.first * p.leaf_stride;
+                    ++lc.leaves;
+                    for (uint32_t s = 0; s < sr.count; ++s, slot += p.leaf_stride) {
+                        int32_t id;
+                        const float d2 = slot_dist<DP>(q, slot, &id);
+                        if (id < 0) continue;
+                        ++lc.points;
+                        if (d2 <= kth) {
+                            const uint32_t pos = atomicAdd(&sm.ncand, 1u);
+                            if (pos < kSoloCand) sm.cand[pos] = make_key(d2, id);
+                        }
+                    }
+                }
+                __syncwarp();
+                const uint32_t nc = min(sm.ncand, kSoloCand);  // at most 32 buckets of <= 32 slots
+                for (uint32_t base = 0; base < nc; base += 32) {
+                    const uint64_t x = base + lane < nc ? sm.cand[base + lane] : ~0ull;
+                    top = warp_merge_low64(top, warp_sort64(x, lane), lane);
+                }
+                kth = key_dist(shfl64(top, p.k - 1));
+            } else {
+                ++lc.nodes;
+                const uint32_t cnt = __popc(wm);
+                if (depth_n + cnt > kSoloStack) {  // cannot happen (see kSoloStack); recorded
+                    stack_error = true;
+                    continue;
+                }
+                // The lowest-numbered descendant ends on top (popped first).
+                if (want) sm.stack[depth_n + cnt - 1 - __popc(wm & ((1u << lane) - 1u))] = first + lane;
+                depth_n += cnt;
+            }
+        }
+        if (lane < p.k) {
+            p.out_idx[static_cast<size_t>(qi) * p.k + lane] = key_index(top);
+            p.out_dist[static_cast<size_t>(qi) * p.k + lane] = key_dist(top);
+        }
+    }
+    if (p.counters) {
+        lc.flush(p.counters);
+        if (stack_error) atomicExch(&p.counters->error, 1);
+    }
+}
+
 // Traversal 3: one box-bounded search per thread, in the batch's locality order.
 template <int DP, int KMAX>
 __global__ void __launch_bounds__(128) kd_box_knn_kernel(const KdParams p, const float* __restrict__ box,
@@ -801,6 +936,8 @@ int kd_box_build_dp(knn_index* ix, cudaStream_t s) {
     return KNN_OK;
 }
 
+inline uint32_t bucket_slots_of(const KdParams& p) { return p.leaf_slots << (p.node_depth - p.stop_depth); }
+
 template <int DP, int KMAX>
 static int launch_kd_group(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, const uint32_t* order,
                            float* seeds, bool self_seed, uint32_t* fb_list, uint32_t* fb_count, float seed_scale,
@@ -852,7 +989,14 @@ static int launch_kd_group(knn_index* ix, const QueryArgs& a, const QueryPlan& p
                                              static_cast<uint32_t>(std::max(per_sm, 1) * sm_count()));
     kern<<<grid, 32 * kGroupWarps, smem, s>>>(gp);
     KNN_LAUNCHED();
-    kd_fallback_kernel<DP, KMAX><<<8 * static_cast<uint32_t>(sm_count()), 128, 0, s>>>(gp);
+    if (bucket_slots_of(p) <= 32) {
+        constexpr size_t solo_smem = 4 * sizeof(SoloWarpSmem);
+        KNN_TRY_CUDA(cudaFuncSetAttribute(kd_solo_kernel<DP, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          static_cast<int>(solo_smem)));
+        kd_solo_kernel<DP, KMAX><<<8 * static_cast<uint32_t>(sm_count()), 128, solo_smem, s>>>(gp);
+    } else {
+        kd_fallback_kernel<DP, KMAX><<<8 * static_cast<uint32_t>(sm_count()), 128, 0, s>>>(gp);
+    }
     KNN_LAUNCHED();
     if (plan.timing) KNN_TRY(ix->timing.end(s));
     return KNN_OK;
