@@ -147,19 +147,28 @@ int seeded_query(knn_index* ix, const knn::QueryArgs& a, const knn::QueryPlan& p
     if (plan.bf16) return dispatch(ix, a, plan, s);
     const knn::Range range("learned-radius search");
     const size_t n = a.count;
-    const uint32_t* order = nullptr;
-    if (plan.reorder && a.count >= 4096) {
-        if (ix->structure == KNN_KD_TREE) KNN_TRY(knn::kd_order(ix, a, s, &order));
-        if (ix->structure == KNN_BALL_TREE) KNN_TRY(knn::ball_order(ix, a, s, &order));
-    }
     KNN_TRY(ix->seed_ws.reserve(knn::carve_bytes({n * 4, n * 4, 256, knn::retry_scratch_bytes(a.count)})));
     knn::Carver c(ix->seed_ws.ptr);
     float* radii = c.take<float>(n);
     uint32_t* list = c.take<uint32_t>(n);
     uint32_t* list_count = c.take<uint32_t>(1);
     void* scratch = c.take<uint8_t>(knn::retry_scratch_bytes(a.count));
+    // The seeds and the locality order depend on the queries alone: the model runs on the index's
+    // second stream while the order is sorted on the caller's, and the search waits for both.
+    KNN_TRY(ix->side.ensure());
+    KNN_TRY_CUDA(cudaEventRecord(ix->side.fork, s));
+    KNN_TRY_CUDA(cudaStreamWaitEvent(ix->side.stream, ix->side.fork, 0));
     KNN_TRY(knn::model_predict(ix->model.as<float>(), ix->dims, a.queries, a.count, a.max_d2, a.radii, radii,
-                               nullptr, s, true));
+                               nullptr, ix->side.stream, true));
+    KNN_TRY_CUDA(cudaEventRecord(ix->side.join, ix->side.stream));
+    const uint32_t* order = nullptr;
+    if (plan.reorder && a.count >= 4096) {
+        // (The group search takes its warps' queries from the order; 16 levels group them as well
+        // as 24 at two radix passes instead of three.)
+        if (ix->structure == KNN_KD_TREE) KNN_TRY(knn::kd_order(ix, a, s, &order, plan.group ? 16u : 24u));
+        if (ix->structure == KNN_BALL_TREE) KNN_TRY(knn::ball_order(ix, a, s, &order));
+    }
+    KNN_TRY_CUDA(cudaStreamWaitEvent(s, ix->side.join, 0));
     // The warp-group k-d search settles or hands on every query itself (no retry rounds).
     // Its seeds may be widened by a factor exp(widen * margin / 2) that the autotuner picks: a
     // miss costs the warp another walk, a wider seed only a few more candidates per query.

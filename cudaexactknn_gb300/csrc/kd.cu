@@ -18,7 +18,7 @@ namespace knn {
 template <uint32_t DP>
 int kd_query_dp(knn_index*, const QueryArgs&, const QueryPlan&, cudaStream_t);
 template <uint32_t DP>
-int kd_order_dp(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
+int kd_order_dp(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**, uint32_t);
 template <uint32_t DP>
 int kd_group_query_dp(knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, float*, uint32_t*, uint32_t*,
                       float, cudaStream_t);
@@ -172,17 +172,17 @@ int kd_box_prepare(knn_index* ix, cudaStream_t s) {
     }
 }
 
-int kd_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order) {
+int kd_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order, uint32_t max_levels) {
     switch (ix->dp) {
-        case 1: return kd_order_dp<1>(ix, a, s, order);
-        case 2: return kd_order_dp<2>(ix, a, s, order);
-        case 3: return kd_order_dp<3>(ix, a, s, order);
-        case 4: return kd_order_dp<4>(ix, a, s, order);
-        case 8: return kd_order_dp<8>(ix, a, s, order);
-        case 16: return kd_order_dp<16>(ix, a, s, order);
-        case 32: return kd_order_dp<32>(ix, a, s, order);
-        case 64: return kd_order_dp<64>(ix, a, s, order);
-        case 128: return kd_order_dp<128>(ix, a, s, order);
+        case 1: return kd_order_dp<1>(ix, a, s, order, max_levels);
+        case 2: return kd_order_dp<2>(ix, a, s, order, max_levels);
+        case 3: return kd_order_dp<3>(ix, a, s, order, max_levels);
+        case 4: return kd_order_dp<4>(ix, a, s, order, max_levels);
+        case 8: return kd_order_dp<8>(ix, a, s, order, max_levels);
+        case 16: return kd_order_dp<16>(ix, a, s, order, max_levels);
+        case 32: return kd_order_dp<32>(ix, a, s, order, max_levels);
+        case 64: return kd_order_dp<64>(ix, a, s, order, max_levels);
+        case 128: return kd_order_dp<128>(ix, a, s, order, max_levels);
         default: return fail(KNN_ERR_UNSUPPORTED, "dims %u", ix->dims);
     }
 }

@@ -277,9 +277,9 @@ static int launch_kd_variant(knn_index* ix, const QueryArgs& a, const QueryPlan&
 // descent steps (stable radix sort on the path bits).  The order lives in the index workspace
 // until the next query.
 template <uint32_t DP>
-int kd_order_dp(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order) {
+int kd_order_dp(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order, uint32_t max_levels) {
     *order = nullptr;
-    const uint32_t levels = std::min<uint32_t>(ix->node_depth, 24);
+    const uint32_t levels = std::min<uint32_t>(ix->node_depth, std::min<uint32_t>(max_levels, 24));
     if (levels == 0) return KNN_OK;
     const size_t nq = a.count;
     const size_t need = carve_bytes({nq * 4, nq * 4, nq * 4, nq * 4, radix_sort_temp_bytes(a.count)});
@@ -309,7 +309,7 @@ int kd_box_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, co
 template <uint32_t DP>
 int kd_query_dp(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s) {
     const uint32_t* order = a.order;
-    if (!order && p.reorder && a.count >= 4096) KNN_TRY(kd_order_dp<DP>(ix, a, s, &order));
+    if (!order && p.reorder && a.count >= 4096) KNN_TRY(kd_order_dp<DP>(ix, a, s, &order, 24));
     if (p.group && !a.count_dev) return kd_group_query_dp<DP>(ix, a, p, order, nullptr, nullptr, nullptr, 1.0f, s);
     if (p.box) return kd_box_query_dp<DP>(ix, a, p, order, s);
     switch (k_class(a.k)) {
@@ -1093,7 +1093,7 @@ int kd_box_prepare_dp<KNN_DP>(knn_index* ix, cudaStream_t s) {
 }
 template int kd_group_query_dp<KNN_DP>(knn_index*, const QueryArgs&, const QueryPlan&, const uint32_t*, float*,
                                         uint32_t*, uint32_t*, float, cudaStream_t);
-template int kd_order_dp<KNN_DP>(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**);
+template int kd_order_dp<KNN_DP>(knn_index*, const QueryArgs&, cudaStream_t, const uint32_t**, uint32_t);
 
 
 // ---- batches of independent sets (one persistent kernel per class of sets) -----------------------

@@ -237,6 +237,25 @@ struct StreamOrder {
     }
 };
 
+// A second stream of the index for work that can run beside the caller's stream within one
+// query (the radius model's seeds beside the locality sort), joined back through events.
+struct SideStream {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    ~SideStream() {
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    int ensure() {
+        if (stream) return KNN_OK;
+        KNN_TRY_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        KNN_TRY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        KNN_TRY_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+        return KNN_OK;
+    }
+};
+
 // knn_query_host's copy streams: the result rows (by far the larger transfer) are copied out in
 // kParts pieces on as many streams at once, so that several copy engines move them.
 struct HostIo {
@@ -329,6 +348,7 @@ struct knn_index {
     knn::DevBuf workspace;
     knn::DevBuf staging;   // device copies of host queries/results (knn_query_host)
     knn::HostIo host_io;   // knn_query_host's copy streams
+    knn::SideStream side;  // the radius model's stream within a learned-radius query
     knn::StreamOrder order_guard;
     knn::DevBuf counters;  // DevCounters
     knn::QueryTiming timing;
@@ -413,7 +433,8 @@ int tc_prepare(knn_index* ix, cudaStream_t s);
 int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 int tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* bad);
 // Locality order of a query batch for the trees (kd_order / ball_order), in the index workspace.
-int kd_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order);
+// k-d: queries sorted by the node they reach after min(max_levels, 24, tree depth) descent steps.
+int kd_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order, uint32_t max_levels = 24);
 int ball_order(knn_index* ix, const QueryArgs& a, cudaStream_t s, const uint32_t** order);
 int kd_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 // Warp-group k-d search from per-query seed radii (kd_kernels.cu); queries it cannot settle go to
