@@ -32,6 +32,7 @@ QF_LEARNED_RADIUS = 4
 QF_BF16_FILTER = 8
 QF_KEEP_ORDER = 16
 QF_TIMING = 32
+QF_FILTER_CODES = 64
 QF_TEST_FILTER_GIVE_UP = 0x40000000
 
 

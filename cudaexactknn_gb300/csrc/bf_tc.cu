@@ -51,6 +51,19 @@
 // The epilogue rounds the left side up (one FMA) and the right side down (once per tile and per
 // change of T'), so the filter can only keep extra candidates.
 //
+// T' itself.  Each query thread buffers the upper bounds below its current T' as 16-bit codes
+// relative to T' (code c stands for the float whose bits are bits(T') - c 2^13, never below the
+// value it records; far values saturate, which only rounds them up).  When a buffer nears full, the
+// warp flushes: per query the largest code c with at least k codes >= c (bisection over its bits)
+// gives the new T' (at least k recorded upper bounds lie at or below it) and the codes >= c stay,
+// re-based by subtracting c (exact).  Any T' at or above the k-th smallest of some set of recorded
+// upper bounds is correct; a lazily tightened one only keeps a few extra candidates, against a
+// heap update per candidate (k up to 128 entries, one thread each) that serialised the epilogue.
+// Where two blocks per SM still fit it (dims <= 32, or small k), T' is instead kept exact by a heap
+// of the k smallest upper bounds per query (one update per candidate below T'): at a few candidates
+// per query and tile that costs less than the flushes (C3's shape); with many, a flush every
+// max(16, k/4) codes costs less than that many heap updates of up to 7 levels (C4's shape).
+//
 // Cell test (centre tiles).  For a cell of centre c' and radius R' (scaled), every point p' of it
 // has |q' - p'| >= |q' - c'| - R', so no point of the cell can reach a query's k nearest when
 //   S_lo = (1-gn)(n_q + n_c) - 2G - 2E(Cmax)  >  (R' + t)^2,   t >= sqrt((T' + c4) / (1 - g)).
@@ -86,7 +99,8 @@ constexpr uint32_t kMaskWords = kMaxCells / 32;
 constexpr uint32_t kBoxMaxDims = 32;  // the tree layout and its box test up to this many dims
 constexpr uint32_t kRowData = 2 * kTileN;  // floats of row data per tile: norms, then (centres) radii
 constexpr uint32_t kNone = 0xFFFFFFFFu;
-constexpr uint32_t kStage = 16;               // accumulator values staged per thread for its hits
+constexpr uint32_t kStage = 16;               // accumulator values staged per thread (half a chunk)
+constexpr uint32_t kCodeShift = 13;           // a bound code's unit: 2^13 float bits (<= 2^-10 relative)
 constexpr uint32_t kCentreBit = 0x80000000u;  // item code: a centre tile
 constexpr uint32_t kBoundary = 0xFFFFFFFEu;   // item code: centre tiles done, mask next
 constexpr uint32_t kEnd = 0xFFFFFFFDu;        // item code: no more items
@@ -139,6 +153,7 @@ struct TcParams {
     const uint32_t* order;       // row -> query index
     const uint32_t* live_count;  // rows in use (device), or null for nq
     uint32_t k, cap;
+    uint32_t codes;              // bound codes buffered per query row (a multiple of 16, >= k + 48)
     uint32_t* cand;              // [nq][cap] padded point rows
     float* cand_v;               // [nq][cap] their tensor-core sums G
     uint32_t* cand_count;        // [nq]; kNone = plain search
@@ -171,6 +186,19 @@ struct BoundHeap {
         at(pos) = x;
     }
 };
+
+// A thread's buffered upper bounds: 16-bit codes relative to its bound T (see the header), four
+// per 8-byte word, word-major in shared memory (word w of row `row` at base[w * kTileM + row]);
+// slots at and past the thread's count hold 0.
+__device__ __forceinline__ uint32_t bound_code(float T, float u) {  // 0 <= u < T
+    return min((__float_as_uint(T) - __float_as_uint(u)) >> kCodeShift, 0xFFFFu);
+}
+__device__ __forceinline__ void put_code(uint16_t* codes, uint32_t row, uint32_t e, uint32_t code) {
+    codes[((e >> 2) * kTileM + row) * 4 + (e & 3)] = static_cast<uint16_t>(code);
+}
+__device__ __forceinline__ uint32_t codes_at_least(uint2 w, uint32_t c) {
+    return ((w.x & 0xFFFFu) >= c) + ((w.x >> 16) >= c) + ((w.y & 0xFFFFu) >= c) + ((w.y >> 16) >= c);
+}
 
 // The tile sequence of a query tile, identical for every role: home tiles [t0, t1), the centre
 // tiles, then (after the mask is complete) the tiles of each kept cell outside [c0, c1].
@@ -234,7 +262,8 @@ struct TileSeq {
 // BD > 0 (tree layout): after the centre test, the kept cells are re-tested against the exact
 // distance from each query to each cell's axis-aligned box (the query's BD scaled coordinates in
 // registers).
-template <uint32_t H, uint32_t ACC, uint32_t BD>
+// HEAP: T' from a heap of k bounds per query row (in the codes' place) instead of buffered codes.
+template <uint32_t H, uint32_t ACC, uint32_t BD, bool HEAP>
 __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p) {
     constexpr uint32_t kCols = ACC * kTileN;
     extern __shared__ uint8_t smem_raw[];
@@ -245,12 +274,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
     uint8_t* sB0 = sA + a_bytes(H);
     uint8_t* sB1 = sB0 + b_bytes(H);
     float* sN = reinterpret_cast<float*>(sB1 + b_bytes(H));       // [2][kRowData] row data
-    uint32_t* sMask = reinterpret_cast<uint32_t*>(sN + 2 * kRowData);  // [kMaskWords] kept cells
+    uint2* sCodes = reinterpret_cast<uint2*>(sN + 2 * kRowData);       // [codes / 4][kTileM] bound codes
+    uint32_t* sMask = reinterpret_cast<uint32_t*>(sCodes + static_cast<size_t>(p.codes / 4) * kTileM);  // [kMaskWords]
     uint32_t* sItem = sMask + kMaskWords;                              // [2] item code per stage
     float* sMeta = reinterpret_cast<float*>(sItem + 2);                // [2] its norm bound (Pmax/Cmax)
     float* sStage = sMeta + 2;                                         // [kStage][kTileM] staged sums
-    float* heap_base = sStage + kStage * kTileM;                       // [k][kTileM]
-    uint64_t* bars = reinterpret_cast<uint64_t*>(heap_base + static_cast<size_t>(p.k) * kTileM);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sStage + kStage * kTileM);
     uint64_t* full = bars;            // [2] tile (operands + row data) landed
     uint64_t* empty = bars + 2;       // [2] operands consumed by the MMAs
     uint64_t* acc_full = bars + 4;    // [2] accumulator ready
@@ -494,9 +523,24 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
             qb[d] = (BD > 0 && good && d < p.dims) ? p.queries[static_cast<size_t>(qi) * p.dims + d] * p.scale : 0.0f;
         const float r2 = fminf(p.radii ? fminf(p.radii[qi], p.max_d2) : p.max_d2, p.seed[qi]);
         const float seed = good ? __fmul_ru(r2, p.s2) : 0.0f;
-        BoundHeap heap{heap_base + row, p.k};
-        for (uint32_t x = 0; x < p.k; ++x) heap.at(x) = seed;
+        // (The seed bounds the k-th distance by itself; the buffer starts empty.)
         float T = seed;
+        uint16_t* codes16 = reinterpret_cast<uint16_t*>(sCodes);
+        // (Heap mode: the heap's k slots in the codes' place.)
+        BoundHeap heap{reinterpret_cast<float*>(sCodes) + row, p.k};
+        if constexpr (HEAP) {
+            for (uint32_t x = 0; x < p.k; ++x) heap.at(x) = seed;
+        } else {
+            for (uint32_t w = 0; w < p.codes / 4; ++w) sCodes[w * kTileM + row] = make_uint2(0u, 0u);
+        }
+        uint32_t nb = 0;  // codes this row buffers
+        uint32_t umax = 0;  // while T is infinite: the largest value buffered (its bits)
+        bool home = true;  // no centre tile of this query tile seen yet
+        // A flush is due once a row buffers this many codes: k for the first one (the seed is
+        // usually loose), then max(16, k/4) more than a flush kept (a stale bound admits extra
+        // candidates), within the room that leaves for one more chunk.
+        uint32_t due = p.k;
+        const uint32_t step = max(16u, p.k / 4);
         const float qup = good ? __fsqrt_ru(__fmul_ru(nq, __fadd_ru(1.0f, b.gn))) : 0.0f;  // >= |q'|
         const float one_m_gn = __fsub_rd(1.0f, b.gn);
         const float a = __fmul_rd(0.5f, one_m_gn);
@@ -509,6 +553,65 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
         auto set_theta = [&]() {
             const float tp = __fmul_ru(T, b.inv_one_m);  // >= T / (1 - g)
             theta = good ? fmaxf(__fsub_rd(theta0, __fmul_ru(0.5f, tp)), -FLT_MAX) : INFINITY;
+        };
+        // Tightens T from the buffered codes (warp-collective; every lane runs the same passes).
+        auto flush = [&]() {
+            if constexpr (HEAP) return;  // the heap's bound is always exact
+            const bool finite = T <= FLT_MAX;
+            if (__all_sync(0xFFFFFFFFu, nb < p.k)) return;
+            const uint32_t words = (nb + 3) / 4;
+            // Words in steps of four (codes is a multiple of 16; words past a row's count hold 0).
+            const uint32_t wmax = (__reduce_max_sync(0xFFFFFFFFu, words) + 3) & ~3u;
+            uint32_t top = 0;
+            for (uint32_t w = 0; w < wmax; ++w) {
+                const uint2 v = sCodes[w * kTileM + row];
+                top = max(top, max(max(v.x & 0xFFFFu, v.x >> 16), max(v.y & 0xFFFFu, v.y >> 16)));
+            }
+            top = __reduce_max_sync(0xFFFFFFFFu, finite ? top : 0u);
+            // The largest code c with at least k codes >= c, bit by bit from the top one present.
+            uint32_t cstar = 0;
+            for (int bit = top ? 31 - __clz(top) : -1; bit >= 0; --bit) {
+                const uint32_t cand = cstar | (1u << bit);
+                uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+                for (uint32_t w = 0; w < wmax; w += 4) {
+                    const uint2 v0 = sCodes[(w + 0) * kTileM + row], v1 = sCodes[(w + 1) * kTileM + row];
+                    const uint2 v2 = sCodes[(w + 2) * kTileM + row], v3 = sCodes[(w + 3) * kTileM + row];
+                    n0 += codes_at_least(v0, cand);
+                    n1 += codes_at_least(v1, cand);
+                    n2 += codes_at_least(v2, cand);
+                    n3 += codes_at_least(v3, cand);
+                }
+                if ((n0 + n1) + (n2 + n3) >= p.k) cstar = cand;
+            }
+            if (!finite) {
+                // An infinite bound carries no codes: the largest value buffered (at least k of
+                // them lie at or below it) becomes T, and the buffer starts again.
+                if (nb >= p.k) {
+                    for (uint32_t w = 0; w < words; ++w) sCodes[w * kTileM + row] = make_uint2(0u, 0u);
+                    nb = 0;
+                    T = __uint_as_float(umax);
+                    set_theta();
+                }
+            } else {
+                // Keep the codes >= cstar, re-based to the new T (their values are unchanged); with
+                // cstar = 0 (T stays) the codes 0, values within one unit of T, make room.
+                const uint32_t keep = max(cstar, 1u);
+                uint32_t kept = 0;
+                for (uint32_t w = 0; w < words; ++w) {
+                    const uint2 v = sCodes[w * kTileM + row];
+                    const uint32_t cc[4] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16};
+#pragma unroll
+                    for (uint32_t e = 0; e < 4; ++e)
+                        if (cc[e] >= keep) put_code(codes16, row, kept++, cc[e] - cstar);
+                }
+                for (uint32_t e = kept; e < 4 * words; ++e) put_code(codes16, row, e, 0u);
+                nb = kept;
+                due = max(p.k, min(kept + step, p.codes - 32));
+                if (cstar) {
+                    T = __uint_as_float(__float_as_uint(T) - (cstar << kCodeShift));
+                    set_theta();
+                }
+            }
         };
         uint32_t count = 0;
         uint32_t* my_cand = p.cand + static_cast<size_t>(live ? r : 0) * p.cap;
@@ -542,6 +645,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
             tc_fence_after();
         };
         auto process = [&](uint32_t item, bool centre) {
+            if (centre && home) {
+                flush();  // the cell test with the tightest bound the home tiles give
+                home = false;
+            }
             const uint32_t s = i & 1;
             const float meta = sMeta[s];
             const float* rd = sN + s * kRowData;
@@ -598,10 +705,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 auto chunk = [&](const uint32_t (&r)[32], uint32_t c) {
                     // The hit mask of all 32 columns first, branch-free, in four independent
                     // partial masks; then, per half of 16 columns with hits, each lane walks its
-                    // own hits (lanes side by side), recording candidates and folding their
-                    // distance upper bounds into its heap.  A hit is tested again against the
-                    // current theta first (theta only rises as T falls; testing against an older,
-                    // lower theta only keeps extra candidates).
+                    // own hits (lanes side by side), recording candidates and their distance
+                    // upper bounds.  A hit is tested again against the current theta first (theta
+                    // only rises as T falls; testing against an older, lower theta only keeps
+                    // extra candidates).
                     uint32_t mp[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
                     for (uint32_t j4 = 0; j4 < 8; ++j4) {
@@ -639,12 +746,23 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                             const float hi = __fmaf_ru(-2.0f, vj, __fadd_ru(E2, __fmul_ru(up_n, __fadd_ru(nq, nj))));
                             const float u = __fmul_ru(fmaxf(hi, 0.0f), up_g);
                             if (u < T) {
-                                heap.replace_top(u);
-                                T = heap.at(0);
-                                set_theta();
+                                if constexpr (HEAP) {
+                                    heap.replace_top(u);
+                                    T = heap.at(0);
+                                    set_theta();
+                                } else if (nb < p.codes) {
+                                    put_code(codes16, row, nb++, bound_code(T, u));
+                                    if (!(T <= FLT_MAX)) umax = max(umax, __float_as_uint(u));
+                                }
                             }
                         }
                     }
+                };
+                // Buffered codes: a flush once some row of the warp is due (which also leaves room
+                // for the next chunk's 32 columns).
+                auto maybe_flush = [&]() {
+                    if constexpr (!HEAP)
+                        if (__any_sync(0xFFFFFFFFu, nb >= due)) flush();
                 };
                 // (The TMEM loads and waits are warp-collective: the warp reconverges before each.)
 #pragma unroll 1
@@ -652,6 +770,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                     tmem_ld32_async(tcol + (c + 1) * 32, rb);
                     chunk(ra, c);
                     __syncwarp();
+                    maybe_flush();
                     tmem_wait_ld(rb);
                     if (c + 2 < kTileN / 32) {
                         if (ACC == 1 && c + 2 == kTileN / 64) half_way();
@@ -659,6 +778,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                     }
                     chunk(rb, c + 1);
                     __syncwarp();
+                    maybe_flush();
                     if (c + 2 < kTileN / 32) tmem_wait_ld(ra);
                 }
             }
@@ -680,6 +800,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_filter_kernel(const TcParams p
                 break;
             }
             if (code == kEnd) {
+                flush();  // the final bound, for the rescoring
                 next = __float_as_uint(sMeta[i & 1]);
                 release(true);
                 break;
@@ -1028,14 +1149,20 @@ __global__ void __launch_bounds__(32 * kRescoreWarps) tc_rescore_kernel(const Re
 }
 
 // Exhaustive search for the queries the filter could not settle (listed in `retry`, count on the
-// device), split over kExhChunks blocks per query: each block scans its share of the point rows
+// device), split over at least kExhChunks blocks per query (more when few queries would leave most
+// of the grid idle; the same count in both kernels): each block scans its share of the point rows
 // with the reference's sequential FP32 distance, appends keys below the query's radius to a shared
 // buffer that is sorted and trimmed to the k smallest whenever it fills (the radius then tightens
 // to the k-th key), and writes its k smallest; a second kernel merges the chunks per query.
 constexpr uint32_t kExhThreads = 256;
 constexpr uint32_t kExhBuf = 2048;
 constexpr uint32_t kExhRound = 4;    // points per thread between buffer checks
-constexpr uint32_t kExhChunks = 8;   // blocks per query
+constexpr uint32_t kExhChunks = 8;      // blocks per query, at least
+constexpr uint32_t kExhMaxChunks = 64;  // and at most
+
+__host__ __device__ __forceinline__ uint32_t exh_chunks(uint32_t nretry, uint32_t blocks) {
+    return nretry ? min(kExhMaxChunks, max(kExhChunks, blocks / nretry)) : kExhChunks;
+}
 
 __device__ __forceinline__ void block_bitonic(uint64_t* buf, uint32_t n) {
     for (uint32_t size = 2; size <= n; size <<= 1) {
@@ -1082,10 +1209,12 @@ __global__ void __launch_bounds__(kExhThreads) tc_exhaustive_kernel(const float*
     __shared__ uint64_t buf[kExhBuf];
     __shared__ uint32_t fill;
     __shared__ uint64_t limit;
-    const uint32_t items = *retry_count * kExhChunks;
-    const uint32_t csize = (prows + kExhChunks - 1) / kExhChunks;
+    const uint32_t nretry = *retry_count;
+    const uint32_t chunks = exh_chunks(nretry, gridDim.x);
+    const uint32_t items = nretry * chunks;
+    const uint32_t csize = (prows + chunks - 1) / chunks;
     for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
-        const uint32_t e = item / kExhChunks, ch = item % kExhChunks;
+        const uint32_t e = item / chunks, ch = item % chunks;
         const uint32_t qi = retry[e];
         float qv[PS];
 #pragma unroll
@@ -1111,22 +1240,25 @@ __global__ void __launch_bounds__(kExhThreads) tc_exhaustive_kernel(const float*
             if (fill + kExhThreads * kExhRound > kExhBuf) block_trim(buf, &fill, &limit, k);
         }
         block_trim(buf, &fill, &limit, k);
-        uint64_t* out = xkeys + (static_cast<size_t>(e) * kExhChunks + ch) * k;
+        uint64_t* out = xkeys + (static_cast<size_t>(e) * chunks + ch) * k;
         for (uint32_t j = threadIdx.x; j < k; j += blockDim.x) out[j] = j < fill ? buf[j] : ~0ull;
         __syncthreads();
     }
 }
 
-// Merges the kExhChunks partial lists of each retried query and writes its row.
+// Merges the partial lists of each retried query and writes its row (launched on the same grid as
+// the scan, so that both count the same chunks; shared memory: the next power of two at or above
+// kExhMaxChunks k keys).
 __global__ void __launch_bounds__(kExhThreads) tc_exhaustive_merge_kernel(uint32_t k, const uint32_t* __restrict__ retry,
                                                                           const uint32_t* __restrict__ retry_count,
                                                                           const float* __restrict__ retry_r2,
                                                                           const uint64_t* __restrict__ xkeys,
                                                                           int32_t* __restrict__ out_idx,
                                                                           float* __restrict__ out_dist) {
-    __shared__ uint64_t buf[kExhChunks * kMaxK];
+    extern __shared__ uint64_t xbuf[];
+    uint64_t* buf = xbuf;
     const uint32_t nretry = *retry_count;
-    const uint32_t m = kExhChunks * k;
+    const uint32_t m = exh_chunks(nretry, gridDim.x) * k;
     uint32_t n2 = 1;
     while (n2 < m) n2 <<= 1;
     for (uint32_t e = blockIdx.x; e < nretry; e += gridDim.x) {
@@ -1683,22 +1815,47 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
     }
 }
 
-size_t filter_smem(uint32_t H, uint32_t k) {
+// Shared memory of the filter apart from its bound codes.
+size_t filter_fixed_smem(uint32_t H) {
     return 1024 + a_bytes(H) + 2 * b_bytes(H) + 2 * kRowData * sizeof(float) + kMaskWords * sizeof(uint32_t) + 16 +
-           (kStage + static_cast<size_t>(k)) * kTileM * 4 + 16 * 8 + 8;
+           kStage * kTileM * 4 + 16 * 8 + 8;
+}
+
+// The heap mode's k floats per query row, where two blocks per SM still fit them.
+bool filter_heap_fits(uint32_t H, uint32_t k) {
+    return 2 * (filter_fixed_smem(H) + static_cast<size_t>((2 * k + 15) & ~15u) * kTileM * 2 + 1024) <= 228 * 1024;
+}
+
+// Bound codes buffered per query row: 4 (k + 32), when two blocks per SM then still fit; else
+// as many as one block's shared memory leaves, up to that (a flush makes room for the next chunk's
+// 32 columns above the k codes it keeps, so fewer than k + 48 leave too little room).  In heap
+// mode, the codes' bytes hold the heap and the pending list instead.
+uint32_t filter_codes(uint32_t H, uint32_t k, bool heap = false) {
+    if (heap) return (2 * k + 15) & ~15u;
+    const uint32_t want = (4 * (k + 32) + 15) & ~15u;
+    const size_t fixed = filter_fixed_smem(H);
+    if (2 * (fixed + static_cast<size_t>(want) * kTileM * 2 + 1024) <= 228 * 1024) return want;
+    const size_t room = fixed < 232448 ? 232448 - fixed : 0;
+    return std::min<uint32_t>(want, static_cast<uint32_t>(room / (kTileM * 2)) & ~15u);
+}
+
+size_t filter_smem(uint32_t H, uint32_t k, bool heap = false) {
+    return filter_fixed_smem(H) + static_cast<size_t>(filter_codes(H, k, heap)) * kTileM * 2;
 }
 
 // The filter allocates all 512 TMEM columns, so a second resident block on the same SM would
 // wait inside tcgen05.alloc; asking for more than half the SM's shared memory keeps one block
 // per SM.
 // One accumulator (two blocks per SM) when two blocks' shared memory fits an SM.
-uint32_t accumulators(uint32_t H, uint32_t k) { return 2 * (filter_smem(H, k) + 1024) <= 228 * 1024 ? 1u : 2u; }
+uint32_t accumulators(uint32_t H, uint32_t k, bool heap) {
+    return 2 * (filter_smem(H, k, heap) + 1024) <= 228 * 1024 ? 1u : 2u;
+}
 
 // A block allocates ACC x 256 TMEM columns of the SM's 512, so more resident blocks than
 // 512 / (ACC x 256) would wait inside tcgen05.alloc: the shared memory asked for caps them at one
 // block per SM (two accumulators) or two (one accumulator).
-size_t filter_launch_smem(uint32_t H, uint32_t k) {
-    return std::max<size_t>(filter_smem(H, k), accumulators(H, k) == 2 ? 120 * 1024 : 80 * 1024);
+size_t filter_launch_smem(uint32_t H, uint32_t k, bool heap) {
+    return std::max<size_t>(filter_smem(H, k, heap), accumulators(H, k, heap) == 2 ? 120 * 1024 : 80 * 1024);
 }
 
 // Layout code of the operand images for `dims` dimensions (see ly_row_bytes).
@@ -1907,7 +2064,8 @@ int launch_descend(uint32_t dp, const float* queries, uint32_t dims, uint32_t ro
 }  // namespace
 
 bool tc_supported(uint32_t dims, uint32_t k) {
-    return dims >= 1 && dims <= kMaxDims && k >= 1 && k <= kMaxK && filter_smem(halves(dims), k) <= 232448;
+    return dims >= 1 && dims <= kMaxDims && k >= 1 && k <= kMaxK && filter_codes(halves(dims), k) >= k + 48 &&
+           filter_smem(halves(dims), k) <= 232448;
 }
 
 // Builds the cells, operand images, norms, FP32 copy, ids and cell balls of an index (once).
@@ -2356,6 +2514,11 @@ static int rescore(RescoreArgs ra, uint32_t count, cudaStream_t s) {
     return KNN_OK;
 }
 
+// The exhaustive search's grid, and its partial-list slots per query batch: at most
+// max(kExhChunks nq, grid) lists of k keys (exh_chunks).
+static uint32_t exh_grid() { return 4u * static_cast<uint32_t>(sm_count()); }
+static size_t exh_slots(uint32_t nq) { return std::max<size_t>(static_cast<size_t>(nq) * kExhChunks, exh_grid()); }
+
 uint32_t tc_default_cap(uint32_t k) { return std::min(4096u, std::max(1024u, 16u * k)); }
 
 int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaStream_t s) {
@@ -2379,7 +2542,7 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
                                             qimg_bytes, qrows * 4ull, qtiles * 16ull,
                                             static_cast<size_t>(nq) * cap * 4, static_cast<size_t>(nq) * cap * 4,
                                             nq * 4ull, nq * 4ull, nq * 4ull, nq * 4ull, nq * 4ull,
-                                            static_cast<size_t>(nq) * kExhChunks * a.k * 8, 256})));
+                                            exh_slots(nq) * a.k * 8, 256})));
     Carver c(ix->tc.ws.ptr);
     uint32_t* k0 = c.take<uint32_t>(nq);
     uint32_t* v0 = c.take<uint32_t>(nq);
@@ -2396,7 +2559,7 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     uint32_t* retry = c.take<uint32_t>(nq);
     float* seed = c.take<float>(nq);
     float* retry_r2 = c.take<float>(nq);
-    uint64_t* xkeys = c.take<uint64_t>(static_cast<size_t>(nq) * kExhChunks * a.k);
+    uint64_t* xkeys = c.take<uint64_t>(exh_slots(nq) * a.k);
     uint32_t* small = c.take<uint32_t>(64);  // [0] retry count, [1] error flag, [2] filter tile counter
     KNN_TRY_CUDA(cudaMemsetAsync(small, 0, 64 * sizeof(uint32_t), s));
 
@@ -2463,6 +2626,9 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     p.live_count = a.count_dev;
     p.k = a.k;
     p.cap = cap;
+    // T' in a heap where two blocks per SM still fit it, unless the plan asks for codes.
+    const bool heap = !plan.tc_codes && filter_heap_fits(H, a.k);
+    p.codes = filter_codes(H, a.k, heap);
     p.cand = cand;
     p.cand_v = cand_v;
     p.cand_count = cnt;
@@ -2475,17 +2641,27 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     // Rows no block settles (a block that gave up) keep these: the plain search within a huge radius.
     KNN_TRY_CUDA(cudaMemsetAsync(cnt, 0xFF, nq * 4ull, s));
     KNN_TRY_CUDA(cudaMemsetAsync(final_t, 0x7F, nq * 4ull, s));
-    const size_t smem = filter_launch_smem(H, a.k);
-    const uint32_t acc = accumulators(H, a.k);
+    const size_t smem = filter_launch_smem(H, a.k, heap);
+    const uint32_t acc = accumulators(H, a.k, heap);
     // Persistent blocks (one or two per SM, as TMEM allows) take query tiles in turn, so that
     // tiles of uneven cost balance across the SMs instead of leaving a partial last wave.
     const uint32_t grid = std::min<uint32_t>(qtiles, (acc == 2 ? 1u : 2u) * static_cast<uint32_t>(sm_count()));
     void (*kern)(const TcParams) = nullptr;
     // Up to 32 dims (tree layout, boxes of 16 or 32 dims): 32- or 64-byte rows; beyond, 128-byte.
-    if (H == 32) kern = acc == 1 ? tc_filter_kernel<32, 1, 16> : tc_filter_kernel<32, 2, 16>;
-    else if (H == 64) kern = acc == 1 ? tc_filter_kernel<64, 1, 32> : tc_filter_kernel<64, 2, 32>;
-    else if (H == 1) kern = acc == 1 ? tc_filter_kernel<1, 1, 0> : tc_filter_kernel<1, 2, 0>;
-    else kern = acc == 1 ? tc_filter_kernel<2, 1, 0> : tc_filter_kernel<2, 2, 0>;
+    if (heap) {  // (one accumulator: the heap mode fits two blocks per SM)
+        if (H == 32) kern = tc_filter_kernel<32, 1, 16, true>;
+        else if (H == 64) kern = tc_filter_kernel<64, 1, 32, true>;
+        else if (H == 1) kern = tc_filter_kernel<1, 1, 0, true>;
+        else kern = tc_filter_kernel<2, 1, 0, true>;
+    } else if (H == 32) {
+        kern = acc == 1 ? tc_filter_kernel<32, 1, 16, false> : tc_filter_kernel<32, 2, 16, false>;
+    } else if (H == 64) {
+        kern = acc == 1 ? tc_filter_kernel<64, 1, 32, false> : tc_filter_kernel<64, 2, 32, false>;
+    } else if (H == 1) {
+        kern = acc == 1 ? tc_filter_kernel<1, 1, 0, false> : tc_filter_kernel<1, 2, 0, false>;
+    } else {
+        kern = acc == 1 ? tc_filter_kernel<2, 1, 0, false> : tc_filter_kernel<2, 2, 0, false>;
+    }
     if ((H >= 32) != T.tree || (H == 32 && T.bd != 16) || (H == 64 && T.bd != 32))
         return fail(KNN_ERR_UNSUPPORTED, "tensor-core filter: layout %u for a %s layout", H, T.tree ? "tree" : "landmark");
     KNN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
@@ -2532,7 +2708,7 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     // Queries whose candidates overflowed, that the 16-bit format could not hold, or whose filter
     // block gave up: exhaustive search over the layout, one block each, within the radius the
     // filter proved (at least k points lie inside it, so the answer is unchanged).
-    const uint32_t eg = 4u * static_cast<uint32_t>(sm_count());
+    const uint32_t eg = exh_grid();
 #define KNN_EXH(P_)                                                                                                \
     case P_:                                                                                                       \
         tc_exhaustive_kernel<P_><<<eg, kExhThreads, 0, s>>>(T.pts.as<float>(), T.ids.as<uint32_t>(),              \
@@ -2545,7 +2721,12 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     }
 #undef KNN_EXH
     KNN_LAUNCHED();
-    tc_exhaustive_merge_kernel<<<eg, kExhThreads, 0, s>>>(a.k, retry, small, retry_r2, xkeys, a.out_idx, a.out_dist);
+    uint32_t n2 = 1;
+    while (n2 < kExhMaxChunks * a.k) n2 <<= 1;
+    KNN_TRY_CUDA(cudaFuncSetAttribute(tc_exhaustive_merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(n2 * 8)));
+    tc_exhaustive_merge_kernel<<<eg, kExhThreads, n2 * 8, s>>>(a.k, retry, small, retry_r2, xkeys, a.out_idx,
+                                                               a.out_dist);
     KNN_LAUNCHED();
     return KNN_OK;
 }

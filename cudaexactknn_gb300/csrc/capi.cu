@@ -113,6 +113,7 @@ int make_plan(const knn_index* ix, const knn_query_opts* o, knn::QueryPlan* p) {
     p->reorder = (o->flags & KNN_QF_KEEP_ORDER) == 0;
     p->timing = (o->flags & KNN_QF_TIMING) != 0;
     p->bf16 = (o->flags & KNN_QF_BF16_FILTER) != 0;
+    p->tc_codes = (o->flags & KNN_QF_FILTER_CODES) != 0;
     p->test_give_up = (o->flags & KNN_QF_TEST_FILTER_GIVE_UP) != 0;
     p->tc_cap = o->reserved;
     p->leaf_scan = o->leaf_scan;

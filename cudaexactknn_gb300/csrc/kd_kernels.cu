@@ -398,21 +398,6 @@ __device__ __forceinline__ float box_bound(const float (&q)[DP], const float* __
     return acc;
 }
 
-// Position of the n-th (0-based) set bit of m (n < popc(m)), by halving on popcounts.
-__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
-    uint32_t pos = 0;
-#pragma unroll
-    for (uint32_t w = 16; w; w >>= 1) {
-        const uint32_t c = __popc(m & ((1u << w) - 1u));
-        if (n >= c) {
-            n -= c;
-            m >>= w;
-            pos += w;
-        }
-    }
-    return pos;
-}
-
 template <int DP, int KMAX>
 __global__ void __launch_bounds__(kGroupWarps * 32) kd_group_kernel(const KdGroupParams gp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -314,4 +314,19 @@ __host__ __device__ __forceinline__ uint32_t log2_ceil(uint32_t v) {
 // Depth of node i in an implicit heap (root depth 0).
 __device__ __forceinline__ uint32_t heap_depth(uint32_t node) { return 31u - __clz(node + 1u); }
 
+// Position of the n-th (0-based) set bit of m (n < popc(m)), by halving on popcounts.
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t w = 16; w; w >>= 1) {
+        const uint32_t c = __popc(m & ((1u << w) - 1u));
+        if (n >= c) {
+            n -= c;
+            m >>= w;
+            pos += w;
+        }
+    }
+    return pos;
+}
+
 }  // namespace knn

@@ -156,6 +156,7 @@ struct DevCounters {
 struct QueryPlan {
     uint32_t block = 0;      // threads per block
     bool heap = false;
+    bool tc_codes = false;   // filter: k-th bound as buffered codes even where a heap fits
     bool sh_nn = false;
     bool sh_stack = false;
     bool reorder = true;
@@ -429,6 +430,7 @@ int bf_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t
 int query_structure(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 // Any index through the 16-bit tensor-core filter with tile skipping (bf_tc.cu).
 bool tc_supported(uint32_t dims, uint32_t k);
+
 int tc_prepare(knn_index* ix, cudaStream_t s);
 int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& p, cudaStream_t s);
 int tc_selftest(uint32_t dims, float* max_rel_err, uint32_t* bad);

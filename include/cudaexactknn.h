@@ -85,6 +85,10 @@ typedef enum knn_structure {
                                     rescore; the same answer as the plain search */
 #define KNN_QF_KEEP_ORDER 16u    /* do not reorder queries for locality */
 #define KNN_QF_TIMING 32u        /* record CUDA events around the query and each of its search kernels */
+#define KNN_QF_FILTER_CODES 64u  /* KNN_QF_BF16_FILTER: keep the filter's running k-th bound as
+                                    buffered 16-bit codes flushed in batches even where a heap per
+                                    query fits (the heap, exact after every candidate, is the
+                                    default where it fits: dims <= 32, or small k up to 64 dims) */
 /* Test only: every tensor-core filter block gives up right after issuing its first point-tile
  * copy, as it does when one of its bounded waits runs out: it drains what it issued, frees its
  * tensor memory, flags the error, and leaves its queries (and the tiles it never took) to the

@@ -21,6 +21,12 @@ def _flags():
     return _lib.QF_BF16_FILTER
 
 
+def _codes():
+    """The running k-th bound as buffered codes also where the heap fits."""
+    from cudaexactknn_gb300 import _lib
+    return _lib.QF_FILTER_CODES
+
+
 @pytest.mark.parametrize("dims", [3, 9, 16, 17, 24, 32, 40, 64, 100, 128])
 def test_tensor_core_selftest(dims):
     """tcgen05.mma over one 128x256 tile matches exact products of the FP16 and BF16 inputs, in
@@ -35,14 +41,17 @@ def test_tensor_core_selftest(dims):
 
 
 @pytest.mark.parametrize("dims", [16, 17, 32, 64, 100, 128])
-@pytest.mark.parametrize("k", [1, 10, 100])
+@pytest.mark.parametrize("k", [1, 10, 100, 128])
 def test_filter_exact(dims, k):
+    """Both forms of the running k-th bound: buffered codes, and the heap where it fits."""
     rng = np.random.default_rng(dims * 1000 + k)
     pts, centres = W.gauss_mix(rng, 6000, dims, 24, 0.3)
     qs, _ = W.gauss_mix(rng, 300, dims, 24, 0.3, centres)
     ix = gu.make_index("bf", pts)
     want = oracle.bf_knn(pts, qs, k, fma=True, threads=8)
-    gu.assert_rows_equal(*gu.run(ix, qs, k, flags=_flags()), *want, what=f"bf16 filter D={dims} k={k}")
+    for codes in (0, _codes()):
+        gu.assert_rows_equal(*gu.run(ix, qs, k, flags=_flags() | codes), *want,
+                             what=f"bf16 filter D={dims} k={k} codes={codes}")
 
 
 @pytest.mark.parametrize("n,nq", [(1, 5), (255, 129), (257, 127), (1025, 1), (3000, 1000)])
@@ -63,7 +72,39 @@ def test_filter_ties_and_duplicates():
     ix = gu.make_index("bf", grid)
     for k in (1, 32, 128):
         want = oracle.bf_knn(grid, qs, k, fma=True, threads=8)
-        gu.assert_rows_equal(*gu.run(ix, qs, k, flags=_flags()), *want, what=f"grid ties k={k}")
+        for codes in (0, _codes()):
+            gu.assert_rows_equal(*gu.run(ix, qs, k, flags=_flags() | codes), *want, what=f"grid ties k={k} codes={codes}")
+
+
+def test_bound_buffer_flushes_on_wide_data():
+    """128 dims, k = 128: the filter (not the plain search) answers, and the buffered k-th bounds
+    are flushed many times per query tile (dense home tiles, then sparse kept cells), with every
+    row exact."""
+    from cudaexactknn_gb300 import knn
+    rng = np.random.default_rng(21)
+    pts, centres = W.gauss_mix(rng, 20000, 128, 32, 0.2)
+    qs, _ = W.gauss_mix(rng, 640, 128, 32, 0.2, centres)
+    ix = gu.make_index("bf", pts)
+    for k in (100, 128):
+        want = oracle.bf_knn(pts, qs, k, fma=True, threads=8)
+        gu.assert_rows_equal(*gu.run(ix, qs, k, flags=_flags()), *want, what=f"D=128 k={k}")
+        c = ix.stats(knn.Query(gu.to_dev(qs), len(qs), float("inf")), k, flags=_flags())
+        assert c.leaves_visited > 0 and c.fallback_queries <= len(qs) // 100, (k, c.leaves_visited, c.fallback_queries)
+
+
+@pytest.mark.parametrize("n", [300, 256 * 8 + 44])
+def test_infinite_seed_bounds(n):
+    """A query whose cell holds fewer than k points starts with an infinite bound: every column
+    is a candidate and its first flush takes the largest buffered value (tree layout, 24 dims: the
+    cells are 256-point tiles and the last one is partial; the queries are the points themselves,
+    so some descend to that cell)."""
+    rng = np.random.default_rng(n)
+    pts = W.uniform(rng, n, 24)
+    ix = gu.make_index("bf", pts)
+    for k in (100, 128):
+        want = oracle.bf_knn(pts, pts, k, fma=True, threads=8)
+        for codes in (0, _codes()):
+            gu.assert_rows_equal(*gu.run(ix, pts, k, flags=_flags() | codes), *want, what=f"n={n} k={k} codes={codes}")
 
 
 def test_candidate_overflow_falls_back_exactly():
@@ -100,7 +141,9 @@ def test_filter_on_trees(structure, dims, k):
     ix = gu.make_index(structure, pts)
     for r2 in (float("inf"), 0.5):
         want = oracle.bf_knn(pts, qs, k, r2, fma=True, threads=8)
-        gu.assert_rows_equal(*gu.run(ix, qs, k, r2, flags=_flags()), *want, what=f"{structure} D={dims} k={k} r2={r2}")
+        for codes in (0, _codes()):
+            gu.assert_rows_equal(*gu.run(ix, qs, k, r2, flags=_flags() | codes), *want,
+                                 what=f"{structure} D={dims} k={k} r2={r2} codes={codes}")
 
 
 def test_clustered_data_skips_tiles():
@@ -158,10 +201,11 @@ def test_persistent_blocks_take_several_query_tiles(structure, dims, k, nq):
         pts, centres = W.gauss_mix(rng, 20000, dims, 32, 0.3)
         qs, _ = W.gauss_mix(rng, nq, dims, 32, 0.3, centres)
     ix = gu.make_index(structure, pts, 1 if structure == "ball" else None)
-    idx, dist = gu.run(ix, qs, k, flags=_flags())
     rows = np.random.default_rng(1).choice(nq, size=1500, replace=False)
     want = oracle.bf_knn(pts, qs[rows], k, fma=True, threads=8)
-    gu.assert_rows_equal(idx[rows], dist[rows], *want, what=f"{structure} D={dims} k={k} nq={nq}")
+    for codes in (0, _codes()):
+        idx, dist = gu.run(ix, qs, k, flags=_flags() | codes)
+        gu.assert_rows_equal(idx[rows], dist[rows], *want, what=f"{structure} D={dims} k={k} nq={nq} codes={codes}")
     ix.close()
 
 
