@@ -1160,8 +1160,10 @@ constexpr uint32_t kExhRound = 4;    // points per thread between buffer checks
 constexpr uint32_t kExhChunks = 8;      // blocks per query, at least
 constexpr uint32_t kExhMaxChunks = 64;  // and at most
 
-__host__ __device__ __forceinline__ uint32_t exh_chunks(uint32_t nretry, uint32_t blocks) {
-    return nretry ? min(kExhMaxChunks, max(kExhChunks, blocks / nretry)) : kExhChunks;
+// More chunks only while each keeps at least kExhMinRows rows: the merge sorts chunks x k keys.
+constexpr uint32_t kExhMinRows = 8192;
+__host__ __device__ __forceinline__ uint32_t exh_chunks(uint32_t nretry, uint32_t blocks, uint32_t prows) {
+    return nretry ? max(kExhChunks, min(min(kExhMaxChunks, blocks / nretry), prows / kExhMinRows)) : kExhChunks;
 }
 
 __device__ __forceinline__ void block_bitonic(uint64_t* buf, uint32_t n) {
@@ -1210,7 +1212,7 @@ __global__ void __launch_bounds__(kExhThreads) tc_exhaustive_kernel(const float*
     __shared__ uint32_t fill;
     __shared__ uint64_t limit;
     const uint32_t nretry = *retry_count;
-    const uint32_t chunks = exh_chunks(nretry, gridDim.x);
+    const uint32_t chunks = exh_chunks(nretry, gridDim.x, prows);
     const uint32_t items = nretry * chunks;
     const uint32_t csize = (prows + chunks - 1) / chunks;
     for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
@@ -1249,7 +1251,8 @@ __global__ void __launch_bounds__(kExhThreads) tc_exhaustive_kernel(const float*
 // Merges the partial lists of each retried query and writes its row (launched on the same grid as
 // the scan, so that both count the same chunks; shared memory: the next power of two at or above
 // kExhMaxChunks k keys).
-__global__ void __launch_bounds__(kExhThreads) tc_exhaustive_merge_kernel(uint32_t k, const uint32_t* __restrict__ retry,
+__global__ void __launch_bounds__(kExhThreads) tc_exhaustive_merge_kernel(uint32_t k, uint32_t prows,
+                                                                          const uint32_t* __restrict__ retry,
                                                                           const uint32_t* __restrict__ retry_count,
                                                                           const float* __restrict__ retry_r2,
                                                                           const uint64_t* __restrict__ xkeys,
@@ -1258,7 +1261,7 @@ __global__ void __launch_bounds__(kExhThreads) tc_exhaustive_merge_kernel(uint32
     extern __shared__ uint64_t xbuf[];
     uint64_t* buf = xbuf;
     const uint32_t nretry = *retry_count;
-    const uint32_t m = exh_chunks(nretry, gridDim.x) * k;
+    const uint32_t m = exh_chunks(nretry, gridDim.x, prows) * k;
     uint32_t n2 = 1;
     while (n2 < m) n2 <<= 1;
     for (uint32_t e = blockIdx.x; e < nretry; e += gridDim.x) {
@@ -2721,12 +2724,13 @@ int bf_tc_query(knn_index* ix, const QueryArgs& a, const QueryPlan& plan, cudaSt
     }
 #undef KNN_EXH
     KNN_LAUNCHED();
-    uint32_t n2 = 1;
-    while (n2 < kExhMaxChunks * a.k) n2 <<= 1;
+    const uint32_t prows = T.ptiles * kTileN;
+    uint32_t n2 = 1;  // the merge's keys: as many chunks as exh_chunks can give, k each
+    while (n2 < std::max(kExhChunks, std::min(kExhMaxChunks, prows / kExhMinRows)) * a.k) n2 <<= 1;
     KNN_TRY_CUDA(cudaFuncSetAttribute(tc_exhaustive_merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(n2 * 8)));
-    tc_exhaustive_merge_kernel<<<eg, kExhThreads, n2 * 8, s>>>(a.k, retry, small, retry_r2, xkeys, a.out_idx,
-                                                               a.out_dist);
+    tc_exhaustive_merge_kernel<<<eg, kExhThreads, n2 * 8, s>>>(a.k, prows, retry, small, retry_r2, xkeys,
+                                                               a.out_idx, a.out_dist);
     KNN_LAUNCHED();
     return KNN_OK;
 }
