@@ -68,9 +68,10 @@ def parse_args():
     ap.add_argument("--configs", default="c1,c3,c4,c5",
                     help="with the default c2 workload: further configurations measured after it and "
                          "reported in the line's `configs` block (comma list, or `none`)")
-    ap.add_argument("--profile-once", choices=["chosen", "plain", "no_model"], default=None,
+    ap.add_argument("--profile-once", choices=["chosen", "plain", "no_model", "build"], default=None,
                     help="set up (train, autotune), then run one query of that form between "
-                         "cudaProfilerStart/Stop and exit (for ncu --profile-from-start off)")
+                         "cudaProfilerStart/Stop and exit (for ncu --profile-from-start off); "
+                         "`build`: the index construction (after one untimed warm-up build)")
     return ap.parse_args()
 
 
@@ -787,6 +788,15 @@ def profile_once(D, args):
     w = workload(args)
     pts = torch.from_numpy(w.points).to(D.dev)
     qs = torch.from_numpy(w.queries).to(D.dev)
+    if args.profile_once == "build":
+        knn.build_index(w.structure, pts, w.depth_skips).close()  # warm-up (module load, pools)
+        torch.cuda.synchronize(D.dev)
+        torch.cuda.profiler.start()
+        index = knn.build_index(w.structure, pts, w.depth_skips)
+        torch.cuda.synchronize(D.dev)
+        torch.cuda.profiler.stop()
+        index.close()
+        return
     index = knn.build_index(w.structure, pts, w.depth_skips)
     query = knn.Query(qs, len(w.queries), w.max_dist2)
     if args.profile_once == "plain":
