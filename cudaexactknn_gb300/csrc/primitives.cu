@@ -48,12 +48,15 @@ __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint32_t
 }
 
 // Stable scatter: each warp owns a contiguous sub-tile and walks it in order, so equal digits
-// keep their input order.
+// keep their input order.  offsets[d * nblocks + b] is the exclusive prefix of digit d's counts
+// over the blocks before b; each block adds the keys of all smaller digits, from the rows' totals
+// (a scan of 256 values per block instead of one serial scan of 256 x nblocks).
 __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n, uint32_t shift,
-    const uint32_t* __restrict__ offsets, uint32_t nblocks, uint32_t* __restrict__ keys_out,
-    uint32_t* __restrict__ vals_out) {
+    const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets, uint32_t nblocks,
+    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out) {
     __shared__ uint32_t h[kSortWarps][256];
+    __shared__ uint32_t digit_sums[kSortWarps];
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     for (uint32_t i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&h[0][0])[i] = 0;
     __syncthreads();
@@ -69,7 +72,19 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     __syncthreads();
     {
         const uint32_t d = threadIdx.x;  // one digit per thread (256 threads)
-        uint32_t run = offsets[static_cast<size_t>(d) * nblocks + blockIdx.x];
+        const size_t last = static_cast<size_t>(d) * nblocks + nblocks - 1;
+        const uint32_t total = offsets[last] + counts[last];  // keys of digit d in the whole pass
+        uint32_t incl = total;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<uint32_t>(o)) incl += v;
+        }
+        if (lane == 31) digit_sums[warp] = incl;
+        __syncthreads();
+        uint32_t below = incl - total;  // smaller digits in this warp
+        for (uint32_t w = 0; w < warp; ++w) below += digit_sums[w];
+        uint32_t run = below + offsets[static_cast<size_t>(d) * nblocks + blockIdx.x];
 #pragma unroll
         for (uint32_t w = 0; w < kSortWarps; ++w) {
             const uint32_t c = h[w][d];
@@ -200,8 +215,8 @@ int radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_
     uint32_t *ki = keys, *vi = vals, *ko = keys_alt, *vo = vals_alt;
     for (int shift = 0; shift < key_bits; shift += 8) {
         radix_hist_kernel<<<nblocks, kSortThreads, 0, s>>>(ki, n, shift, counts, nblocks);
-        scan_rows_kernel<<<1, 1024, 0, s>>>(counts, offsets, 256 * nblocks);
-        radix_scatter_kernel<<<nblocks, kSortThreads, 0, s>>>(ki, vi, n, shift, offsets, nblocks, ko, vo);
+        scan_rows_kernel<<<256, 1024, 0, s>>>(counts, offsets, nblocks);  // one row per digit
+        radix_scatter_kernel<<<nblocks, kSortThreads, 0, s>>>(ki, vi, n, shift, counts, offsets, nblocks, ko, vo);
         KNN_LAUNCHED_N(3);
         uint32_t* t = ki;
         ki = ko;

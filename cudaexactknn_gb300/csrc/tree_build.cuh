@@ -9,7 +9,8 @@
 // segmented partition per level moves each other order's entries to the child segments.
 //
 // Per level: side flags from the split order, then for the other orders
-//   count left flags per tile -> exclusive scan of the tile counts -> per-position prefix G
+//   count left flags per tile -> exclusive scan of the tile counts (up to kDirectBlocks tiles:
+//   each tile sums the counts before it itself) -> per-position prefix G
 //   -> scatter to  off + (G[p] - G[off])                   (left child)
 //               or off + left + (p - off) - (G[p] - G[off]) (right child).
 #pragma once
@@ -23,6 +24,9 @@ namespace {  // each including translation unit gets its own copy
 constexpr uint32_t kThreads = 256;
 constexpr uint32_t kItems = 8;
 constexpr uint32_t kTile = kThreads * kItems;  // positions per partition block
+// Up to this many partition blocks per order, each block sums the counts of the blocks before it
+// itself (at most kDirectBlocks / kThreads loads a thread) instead of a separate scan launch.
+constexpr uint32_t kDirectBlocks = 4096;
 
 // keys[i] = orderable(points[i][dim]), vals[i] = i.
 __global__ void extract_keys_kernel(const float* __restrict__ pts, uint32_t n, uint32_t dims, uint32_t dim,
@@ -87,10 +91,13 @@ __global__ void __launch_bounds__(kThreads) flag_count_kernel(const OrderSet os,
     }
 }
 
+// bpre: the exclusive scan of the block counts, or null: the block sums bcnt's entries before it.
 __global__ void __launch_bounds__(kThreads) flag_prefix_kernel(const OrderSet os, const uint8_t* __restrict__ side,
                                                                uint32_t n, uint32_t nblk,
-                                                               const uint32_t* __restrict__ bpre) {
+                                                               const uint32_t* __restrict__ bpre,
+                                                               const uint32_t* __restrict__ bcnt) {
     __shared__ uint32_t warp_tot[kThreads / 32];
+    __shared__ uint32_t warp_before[kThreads / 32];
     const uint32_t y = blockIdx.y;
     const uint32_t* ord = os.cur[y];
     const uint32_t base = blockIdx.x * kTile + threadIdx.x * kItems;
@@ -110,8 +117,22 @@ __global__ void __launch_bounds__(kThreads) flag_prefix_kernel(const OrderSet os
         if (lane >= static_cast<uint32_t>(o)) incl += v;
     }
     if (lane == 31) warp_tot[warp] = incl;
-    __syncthreads();
-    uint32_t before = bpre[static_cast<size_t>(y) * nblk + blockIdx.x];
+    uint32_t before;
+    if (bpre) {
+        __syncthreads();
+        before = bpre[static_cast<size_t>(y) * nblk + blockIdx.x];
+    } else {
+        const uint32_t* row = bcnt + static_cast<size_t>(y) * nblk;
+        uint32_t part = 0;
+        for (uint32_t j = threadIdx.x; j < blockIdx.x; j += kThreads) part += row[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
+        if (lane == 0) warp_before[warp] = part;
+        __syncthreads();
+        before = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < kThreads / 32; ++w) before += warp_before[w];
+    }
     for (uint32_t w = 0; w < warp; ++w) before += warp_tot[w];
     uint32_t run = before + incl - c;
     uint32_t* g = os.g[y];
@@ -227,8 +248,9 @@ inline int partition_orders(Scratch& sc, const uint32_t* which, uint32_t count, 
     dim3 gb(sc.nblk, count);
     flag_count_kernel<<<gb, kThreads, 0, s>>>(os, sc.side, n, sc.nblk, sc.bcnt);
     KNN_LAUNCHED();
-    KNN_TRY(scan_rows_exclusive(sc.bcnt, sc.bpre, count, sc.nblk, s));
-    flag_prefix_kernel<<<gb, kThreads, 0, s>>>(os, sc.side, n, sc.nblk, sc.bpre);
+    const bool direct = sc.nblk <= kDirectBlocks;
+    if (!direct) KNN_TRY(scan_rows_exclusive(sc.bcnt, sc.bpre, count, sc.nblk, s));
+    flag_prefix_kernel<<<gb, kThreads, 0, s>>>(os, sc.side, n, sc.nblk, direct ? nullptr : sc.bpre, sc.bcnt);
     KNN_LAUNCHED();
     dim3 gp(ceil_div(n, 256), count);
     partition_scatter_kernel<<<gp, 256, 0, s>>>(os, sc.side, node_of, off, size, n);
