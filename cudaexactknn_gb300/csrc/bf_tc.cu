@@ -53,8 +53,9 @@
 //
 // T' itself.  Each query thread buffers the upper bounds below its current T' as 16-bit codes
 // relative to T' (code c stands for the float whose bits are bits(T') - c 2^13, never below the
-// value it records; far values saturate, which only rounds them up).  When a buffer nears full, the
-// warp flushes: per query the largest code c with at least k codes >= c (bisection over its bits)
+// value it records; far values saturate, which only rounds them up).  Once a row holds k codes
+// (the first time) or max(16, k/4) more than its last flush kept, its warp flushes: per query the
+// largest code c with at least k codes >= c (bisection over its bits)
 // gives the new T' (at least k recorded upper bounds lie at or below it) and the codes >= c stay,
 // re-based by subtracting c (exact).  Any T' at or above the k-th smallest of some set of recorded
 // upper bounds is correct; a lazily tightened one only keeps a few extra candidates, against a
