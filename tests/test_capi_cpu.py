@@ -159,6 +159,19 @@ def test_ctypes_signatures_match_the_header():
         assert len(_lib._SIGNATURES[name]) == count, name
 
 
+def test_query_flags_match_the_header():
+    """Every KNN_QF_* flag of the header has the same value in the Python mirror (QF_*), and the
+    flags are distinct bits."""
+    import re
+    text = open(os.path.join(ROOT, "include", "cudaexactknn.h")).read()
+    flags = {m.group(1): int(m.group(2), 0) for m in re.finditer(r"#define KNN_(QF_\w+)\s+(0x[0-9a-fA-F]+|\d+)u", text)}
+    assert len(flags) >= 8, flags
+    for name, value in flags.items():
+        assert getattr(_lib, name) == value, name
+    values = list(flags.values())
+    assert all(v & (v - 1) == 0 for v in values) and len(set(values)) == len(values)
+
+
 def test_ctypes_structs_match_the_c_layout(tmp_path):
     """The Python mirrors of the header's structs have the C compiler's size and field offsets."""
     structs = {"knn_query_opts": _lib.QueryOpts, "knn_query_counters": _lib.QueryCounters,
